@@ -1,0 +1,143 @@
+"""ctypes binding of the C ABI in include/axr.h (axiomr_gb300/_bin/libaxr.so).
+
+The library is the only implementation of the draw path: if it cannot be built or
+loaded, every call raises; there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import build as _build
+
+AXR_OK = 0
+STATUS_NAMES = {0: "AXR_OK", 1: "AXR_E_INVALID", 2: "AXR_E_OOM", 3: "AXR_E_BUDGET", 4: "AXR_E_TIMEOUT",
+                5: "AXR_E_CUDA", 6: "AXR_E_UNSUPPORTED", 7: "AXR_E_CAPACITY"}
+
+
+class AxrError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("diffuse", C.c_void_p), ("bump", C.c_void_p), ("metallic", C.c_void_p),
+                ("roughness", C.c_void_p), ("ao", C.c_void_p), ("specular_exponent", C.c_float)]
+
+
+class GroupDesc(C.Structure):
+    _fields_ = [("start_face", C.c_uint32), ("face_count", C.c_uint32), ("material", C.c_uint32)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("positions", C.c_void_p), ("uvs", C.c_void_p),
+                ("normals", C.c_void_p), ("tangents", C.c_void_p), ("bitangents", C.c_void_p),
+                ("num_faces", C.c_uint32), ("indices", C.c_void_p), ("num_groups", C.c_uint32),
+                ("groups", C.c_void_p), ("num_materials", C.c_uint32), ("materials", C.c_void_p)]
+
+
+class ShaderDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("light_direction", C.c_float * 3), ("light_color", C.c_float * 3)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("view_proj", C.c_float * 16), ("viewport", C.c_float * 16), ("position", C.c_float * 3)]
+
+
+class DrawDesc(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("framebuffer", C.c_void_p), ("model", C.c_float * 16),
+                ("camera", CameraDesc), ("shader", ShaderDesc)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("draws", C.c_uint32), ("pad_", C.c_uint32), ("geometry_ms", C.c_double), ("large_ms", C.c_double),
+                ("resolve_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+
+
+class DrawStats(C.Structure):
+    _fields_ = [("triangles", C.c_uint64), ("fragments", C.c_uint64), ("large", C.c_uint64), ("tiles", C.c_uint64)]
+
+
+P = C.c_void_p
+FP = C.POINTER(C.c_float)
+U8P = C.POINTER(C.c_uint8)
+PP = C.POINTER(C.c_void_p)
+S = C.c_int
+
+# name -> (restype, argtypes); every function the header declares
+SIGNATURES = {
+    "axr_context_create": (S, [C.c_int32, PP]),
+    "axr_context_destroy": (None, [P]),
+    "axr_last_error": (C.c_char_p, [P]),
+    "axr_context_stream": (P, [P]),
+    "axr_context_set_stream": (S, [P, P]),
+    "axr_sync": (S, [P]),
+    "axr_reserve": (S, [P, C.c_uint32]),
+    "axr_host_alloc": (P, [C.c_size_t]),
+    "axr_host_free": (None, [P]),
+    "axr_texture_create": (S, [P, P, C.c_int32, C.c_int32, PP]),
+    "axr_texture_update": (S, [P, P, P]),
+    "axr_texture_destroy": (None, [P, P]),
+    "axr_mesh_create": (S, [P, P, PP]),
+    "axr_mesh_update": (S, [P, P, P]),
+    "axr_mesh_destroy": (None, [P, P]),
+    "axr_framebuffer_create": (S, [P, C.c_int32, C.c_int32, PP]),
+    "axr_framebuffer_destroy": (None, [P, P]),
+    "axr_framebuffer_clear_color": (S, [P, P, C.c_uint8, C.c_uint8, C.c_uint8, C.c_uint8]),
+    "axr_framebuffer_clear_depth": (S, [P, P, C.c_float]),
+    "axr_framebuffer_read": (S, [P, P, P, P]),
+    "axr_framebuffer_read_async": (S, [P, P, P, P]),
+    "axr_framebuffer_write": (S, [P, P, P, P]),
+    "axr_framebuffer_size": (S, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "axr_framebuffer_device_pointers": (S, [P, PP, PP]),
+    "axr_set_shader": (S, [P, P]),
+    "axr_set_camera": (S, [P, P]),
+    "axr_set_framebuffer": (S, [P, P]),
+    "axr_draw_mesh": (S, [P, P, P]),
+    "axr_draw_batch": (S, [P, P, C.c_int32]),
+    "axr_graph_begin": (S, [P]),
+    "axr_graph_end": (S, [P, PP]),
+    "axr_graph_launch": (S, [P, P]),
+    "axr_graph_destroy": (None, [P]),
+    "axr_camera_matrices": (S, [P, P, C.c_float, C.c_float, P, P, P]),
+    "axr_viewport_matrix": (S, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]),
+    "axr_stats_enable": (S, [P, C.c_int32]),
+    "axr_stats_read": (S, [P, P]),
+    "axr_profile_enable": (S, [P, C.c_int32]),
+    "axr_profile_read": (S, [P, P]),
+    "axr_debug_triangles": (S, [P, P, P, P, C.c_int32, C.c_int32, P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "axr_debug_sample": (S, [P, P, P, C.c_int32, P]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_needed: bool = True):
+    """Load libaxr.so (building it first when sources are newer), bind all symbols."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build() if build_if_needed else _build.LIB
+            if not path.exists():
+                raise OSError(f"{path} not found: the CUDA extension has not been built")
+            lib = C.CDLL(str(path))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def check(status: int, ctx=None) -> None:
+    if status != AXR_OK:
+        lib = load()
+        msg = lib.axr_last_error(ctx).decode(errors="replace") if lib else ""
+        raise AxrError(status, msg)

@@ -1,0 +1,408 @@
+"""Python mirror of AxiomR's renderer API over the C ABI (include/axr.h).
+
+Names and argument meaning follow the reference classes:
+  Framebuffer     include/framebuffer.hpp  (BGRA8 colour + float depth, row 0 at the bottom)
+  Texture         include/texture.hpp      (RGBA8, row 0 first)
+  Mesh / Material include/mesh.hpp         (from arrays; OBJ loading is the caller's)
+  Camera          include/camera.hpp       (matrices from position/target/fov/aspect)
+  FlatShader, PhongShader, PBRShader       include/shaders/shaders.hpp
+  BlinnPhongShader, GouraudShader          this library's own shaders
+  TiledPipeline   include/tiled_pipeline.hpp (setShader/setCamera/setFramebuffer/drawMesh)
+  Renderer.drawMesh                        src/renderer.cpp:16-19
+Every call runs the CUDA library; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import AxrError, CameraDesc, DrawDesc, DrawStats, GroupDesc, MaterialDesc, MeshDesc, ShaderDesc, check
+
+FLAT, PHONG, PBR, BLINN_PHONG, GOURAUD = 0, 1, 2, 3, 4
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+class Context:
+    """One CUDA stream, pipeline state and scratch arena on one device (axr_context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.axr_context_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.axr_context_stream(self.handle) or 0)
+
+    def sync(self) -> None:
+        check(self.lib.axr_sync(self.handle), self.handle)
+
+    def reserve(self, max_faces: int) -> None:
+        check(self.lib.axr_reserve(self.handle, int(max_faces)), self.handle)
+
+    def stats(self, enable: Optional[bool] = None):
+        if enable is not None:
+            check(self.lib.axr_stats_enable(self.handle, 1 if enable else 0), self.handle)
+            return None
+        s = DrawStats()
+        check(self.lib.axr_stats_read(self.handle, C.byref(s)), self.handle)
+        return {"triangles": s.triangles, "fragments": s.fragments, "large": s.large, "tiles": s.tiles}
+
+    def profile(self, enable: Optional[bool] = None):
+        """Enable/disable stage timing, or (no argument) read and reset it."""
+        if enable is not None:
+            check(self.lib.axr_profile_enable(self.handle, 1 if enable else 0), self.handle)
+            return None
+        pr = _lib.Profile()
+        check(self.lib.axr_profile_read(self.handle, C.byref(pr)), self.handle)
+        return {"draws": pr.draws, "geometry_ms": pr.geometry_ms, "large_ms": pr.large_ms,
+                "resolve_ms": pr.resolve_ms, "kernel_launches": pr.kernel_launches}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.axr_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Texture:
+    """RGBA8 texture (Texture, include/texture.hpp); `rgba` is (H, W, 4) uint8, row 0 first."""
+
+    def __init__(self, ctx: Context, rgba: np.ndarray):
+        rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+        if rgba.ndim != 3 or rgba.shape[2] != 4:
+            raise ValueError("texture must be (H, W, 4) uint8")
+        self.ctx = ctx
+        self.height, self.width = rgba.shape[:2]
+        h = C.c_void_p()
+        check(ctx.lib.axr_texture_create(ctx.handle, rgba.ctypes.data, self.width, self.height, C.byref(h)),
+              ctx.handle)
+        self.handle = h
+
+    def update(self, rgba: np.ndarray) -> None:
+        rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+        self._pending = rgba
+        check(self.ctx.lib.axr_texture_update(self.ctx.handle, self.handle, rgba.ctypes.data), self.ctx.handle)
+
+    def sample(self, uv: np.ndarray) -> np.ndarray:
+        """Texture::sample at (n, 2) uv -> (n, 4) float32 (runs on the GPU)."""
+        uvf = _f32(uv).reshape(-1, 2)
+        out = np.zeros((uvf.shape[0], 4), np.float32)
+        check(self.ctx.lib.axr_debug_sample(self.ctx.handle, self.handle, uvf.ctypes.data, uvf.shape[0],
+                                            out.ctypes.data), self.ctx.handle)
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.axr_texture_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class Material:
+    """Material (include/mesh.hpp:20-34): the textures the shaders read + Ns."""
+    diffuse: Optional[Texture] = None
+    bump: Optional[Texture] = None
+    metallic: Optional[Texture] = None
+    roughness: Optional[Texture] = None
+    ao: Optional[Texture] = None
+    specular_exponent: float = 1.0
+
+    def desc(self) -> MaterialDesc:
+        t = lambda x: x.handle if x is not None else None  # noqa: E731
+        return MaterialDesc(t(self.diffuse), t(self.bump), t(self.metallic), t(self.roughness), t(self.ao),
+                            float(self.specular_exponent))
+
+
+class Mesh:
+    """Device-resident mesh (Mesh, include/mesh.hpp) from vertex/face arrays."""
+
+    def __init__(self, ctx: Context, positions, uvs, normals, indices, groups=None, materials: Sequence = (),
+                 tangents=None, bitangents=None):
+        self.ctx = ctx
+        self._arrays = self._pack(positions, uvs, normals, indices, tangents, bitangents)
+        nf = self._arrays["indices"].shape[0]
+        self.groups = np.asarray(groups if groups is not None else [[0, nf, 0]], dtype=np.uint32).reshape(-1, 3)
+        self.materials = list(materials) if materials else [Material()]
+        self.num_faces = nf
+        self.num_vertices = self._arrays["positions"].shape[0]
+        desc, keep = self._desc(self._arrays)
+        h = C.c_void_p()
+        check(ctx.lib.axr_mesh_create(ctx.handle, C.byref(desc), C.byref(h)), ctx.handle)
+        self.handle = h
+
+    @staticmethod
+    def _pack(positions, uvs, normals, indices, tangents, bitangents):
+        a = {"positions": _f32(positions).reshape(-1, 3), "uvs": _f32(uvs).reshape(-1, 2),
+             "normals": _f32(normals).reshape(-1, 3),
+             "indices": np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3),
+             "tangents": None if tangents is None else _f32(tangents).reshape(-1, 3),
+             "bitangents": None if bitangents is None else _f32(bitangents).reshape(-1, 3)}
+        return a
+
+    def _desc(self, a):
+        g = (GroupDesc * max(1, len(self.groups)))(*[GroupDesc(int(s), int(c), int(m)) for s, c, m in self.groups])
+        mats = (MaterialDesc * max(1, len(self.materials)))(*[m.desc() for m in self.materials])
+        d = MeshDesc(a["positions"].shape[0], _ptr(a["positions"]), _ptr(a["uvs"]), _ptr(a["normals"]),
+                     _ptr(a["tangents"]), _ptr(a["bitangents"]), a["indices"].shape[0], _ptr(a["indices"]),
+                     len(self.groups), C.addressof(g), len(self.materials), C.addressof(mats))
+        return d, (g, mats)
+
+    @classmethod
+    def from_workload(cls, ctx: Context, mesh, textures: Optional[dict] = None):
+        """Build from an axiomr_gb300.workloads.Mesh, uploading its material textures."""
+        textures = {} if textures is None else textures
+        mats = []
+        for m in mesh.materials:
+            def tex(img):
+                if img is None:
+                    return None
+                key = id(img)
+                if key not in textures:
+                    textures[key] = Texture(ctx, img)
+                return textures[key]
+            mats.append(Material(tex(m.diffuse), tex(m.bump), tex(m.metallic), tex(m.roughness), tex(m.ao),
+                                 m.specular_exponent))
+        obj = cls(ctx, mesh.positions, mesh.uvs, mesh.normals, mesh.indices, mesh.groups, mats,
+                  mesh.tangents, mesh.bitangents)
+        obj._textures = textures
+        return obj
+
+    def update(self, positions, uvs, normals, indices, tangents=None, bitangents=None) -> None:
+        """Re-upload all arrays (same counts), asynchronously on the context stream."""
+        a = self._pack(positions, uvs, normals, indices, tangents, bitangents)
+        desc, keep = self._desc(a)
+        self._pending = (a, keep)
+        check(self.ctx.lib.axr_mesh_update(self.ctx.handle, self.handle, C.byref(desc)), self.ctx.handle)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.axr_mesh_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Framebuffer:
+    """BGRA8 + float depth framebuffer (Framebuffer, include/framebuffer.hpp)."""
+
+    def __init__(self, ctx: Context, width: int, height: int):
+        self.ctx = ctx
+        self.width, self.height = int(width), int(height)
+        h = C.c_void_p()
+        check(ctx.lib.axr_framebuffer_create(ctx.handle, self.width, self.height, C.byref(h)), ctx.handle)
+        self.handle = h
+
+    def clearColor(self, r: int, g: int, b: int, a: int) -> None:
+        check(self.ctx.lib.axr_framebuffer_clear_color(self.ctx.handle, self.handle, r, g, b, a), self.ctx.handle)
+
+    def clearDepth(self, value: float = float("inf")) -> None:
+        check(self.ctx.lib.axr_framebuffer_clear_depth(self.ctx.handle, self.handle, value), self.ctx.handle)
+
+    def read(self, bgra: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None):
+        """(bgra (H, W, 4) uint8, depth (H, W) float32), blocking."""
+        bgra = np.empty((self.height, self.width, 4), np.uint8) if bgra is None else bgra
+        depth = np.empty((self.height, self.width), np.float32) if depth is None else depth
+        check(self.ctx.lib.axr_framebuffer_read(self.ctx.handle, self.handle, bgra.ctypes.data, depth.ctypes.data),
+              self.ctx.handle)
+        return bgra, depth
+
+    def write(self, bgra: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None) -> None:
+        b = None if bgra is None else np.ascontiguousarray(bgra, np.uint8)
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+        check(self.ctx.lib.axr_framebuffer_write(self.ctx.handle, self.handle, _ptr(b), _ptr(d)), self.ctx.handle)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.axr_framebuffer_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Camera:
+    """Camera(position, target, fov, aspect) + update(0) (src/camera.cpp:30-100)."""
+
+    def __init__(self, position=(0.0, 0.0, 0.0), target=(0.0, 0.0, -1.0), fov: float = 60.0,
+                 aspect: float = 16.0 / 9.0, viewport=(0, 0, 800, 600)):
+        self.position = tuple(float(v) for v in position)
+        self.target = tuple(float(v) for v in target)
+        self.fov = float(fov)
+        self.aspect = float(aspect)
+        self.viewport = tuple(int(v) for v in viewport)
+        lib = _lib.load()
+        self.view = np.zeros(16, np.float32)
+        self.projection = np.zeros(16, np.float32)
+        self.view_proj = np.zeros(16, np.float32)
+        pos = _f32(self.position)
+        tgt = _f32(self.target)
+        check(lib.axr_camera_matrices(pos.ctypes.data, tgt.ctypes.data, self.fov, self.aspect, self.view.ctypes.data,
+                                      self.projection.ctypes.data, self.view_proj.ctypes.data))
+        self.viewport_matrix = np.zeros(16, np.float32)
+        check(lib.axr_viewport_matrix(*self.viewport, self.viewport_matrix.ctypes.data))
+
+    @classmethod
+    def from_workload(cls, cam):
+        return cls(cam.position, cam.target, cam.fov_degrees, cam.aspect, cam.viewport)
+
+    @classmethod
+    def from_matrices(cls, view_proj, position, viewport=(0, 0, 1, 1)):
+        """A camera with a given view-projection matrix (16 floats, column-major) and eye
+        position, e.g. matrices computed elsewhere."""
+        cam = cls.__new__(cls)
+        cam.position = tuple(float(v) for v in position)
+        cam.target = None
+        cam.fov = cam.aspect = None
+        cam.viewport = tuple(int(v) for v in viewport)
+        cam.view = cam.projection = None
+        cam.view_proj = _f32(view_proj).reshape(16).copy()
+        cam.viewport_matrix = np.zeros(16, np.float32)
+        check(_lib.load().axr_viewport_matrix(*cam.viewport, cam.viewport_matrix.ctypes.data))
+        return cam
+
+    def desc(self) -> CameraDesc:
+        return CameraDesc((C.c_float * 16)(*self.view_proj), (C.c_float * 16)(*self.viewport_matrix),
+                          (C.c_float * 3)(*self.position))
+
+
+@dataclasses.dataclass
+class Shader:
+    kind: int
+    lightDirection: tuple = (0.0, -1.0, 0.0)
+    lightColor: tuple = (0.6, 0.6, 0.6)
+
+    def desc(self) -> ShaderDesc:
+        return ShaderDesc(int(self.kind), (C.c_float * 3)(*self.lightDirection), (C.c_float * 3)(*self.lightColor))
+
+
+def FlatShader(lightDirection=(0.0, -1.0, 0.0)) -> Shader:
+    return Shader(FLAT, lightDirection)
+
+
+def PhongShader(lightDirection=(0.0, -1.0, 0.0), lightColor=(0.6, 0.6, 0.6)) -> Shader:
+    return Shader(PHONG, lightDirection, lightColor)
+
+
+def PBRShader(lightDirection=(0.0, -1.0, 0.0), lightColor=(5.6, 5.6, 5.6)) -> Shader:
+    return Shader(PBR, lightDirection, lightColor)
+
+
+def BlinnPhongShader(lightDirection=(0.0, -1.0, 0.0), lightColor=(0.6, 0.6, 0.6)) -> Shader:
+    return Shader(BLINN_PHONG, lightDirection, lightColor)
+
+
+def GouraudShader() -> Shader:
+    return Shader(GOURAUD)
+
+
+def _model(m) -> np.ndarray:
+    return _f32(np.eye(4) if m is None else m).reshape(16)
+
+
+class TiledPipeline:
+    """TiledPipeline (include/tiled_pipeline.hpp:58-62) on the GPU."""
+
+    def __init__(self, ctx: Context, camera: Optional[Camera] = None, framebuffer: Optional[Framebuffer] = None):
+        self.ctx = ctx
+        if camera is not None:
+            self.setCamera(camera)
+        if framebuffer is not None:
+            self.setFramebuffer(framebuffer)
+
+    def setShader(self, shader: Optional[Shader]) -> None:
+        d = shader.desc() if shader is not None else None
+        check(self.ctx.lib.axr_set_shader(self.ctx.handle, C.byref(d) if d is not None else None), self.ctx.handle)
+
+    def setCamera(self, camera: Optional[Camera]) -> None:
+        d = camera.desc() if camera is not None else None
+        check(self.ctx.lib.axr_set_camera(self.ctx.handle, C.byref(d) if d is not None else None), self.ctx.handle)
+
+    def setFramebuffer(self, fb: Optional[Framebuffer]) -> None:
+        check(self.ctx.lib.axr_set_framebuffer(self.ctx.handle, fb.handle if fb is not None else None),
+              self.ctx.handle)
+
+    def drawMesh(self, modelMatrix, mesh: Mesh) -> None:
+        m = _model(modelMatrix)
+        check(self.ctx.lib.axr_draw_mesh(self.ctx.handle, mesh.handle, m.ctypes.data), self.ctx.handle)
+
+    def debugTriangles(self, mesh: Mesh, modelMatrix, view_proj, width: int, height: int,
+                       capacity: Optional[int] = None) -> np.ndarray:
+        """Clip-stage output records, sorted by draw order: (n, 14) with column 0 the tag."""
+        cap = int(capacity if capacity is not None else mesh.num_faces * 8 + 16)
+        out = np.zeros((cap, 14), np.float32)
+        cnt = C.c_uint32(0)
+        m = _model(modelMatrix)
+        vp = _f32(view_proj).reshape(16)
+        check(self.ctx.lib.axr_debug_triangles(self.ctx.handle, mesh.handle, m.ctypes.data, vp.ctypes.data,
+                                               int(width), int(height), out.ctypes.data, cap, C.byref(cnt)),
+              self.ctx.handle)
+        rec = out[: min(cnt.value, cap)]
+        order = np.argsort(rec[:, 0].view(np.uint32), kind="stable")
+        return rec[order]
+
+
+class Renderer:
+    """Renderer::drawMesh (src/renderer.cpp:16-19) delegating to its pipeline."""
+
+    def __init__(self, pipeline: TiledPipeline):
+        self.pipeline = pipeline
+
+    def drawMesh(self, transMat, mesh: Mesh) -> None:
+        self.pipeline.drawMesh(transMat, mesh)
+
+
+def render_scene(ctx: Context, scene, framebuffer: Optional[Framebuffer] = None, mesh: Optional[Mesh] = None,
+                 bgra: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None, view_proj=None):
+    """Draw an axiomr_gb300.workloads.Scene as the reference renderer's frame does
+    (clearColor, clearDepth, drawMesh; src/renderer.cpp:124-126) unless an initial
+    framebuffer is given; returns (bgra, depth) read back to the host. `view_proj`
+    overrides the matrix computed from the scene camera."""
+    fb = framebuffer or Framebuffer(ctx, scene.width, scene.height)
+    m = mesh or Mesh.from_workload(ctx, scene.mesh)
+    if bgra is not None or depth is not None:
+        fb.write(bgra, depth)
+    else:
+        b, g, r, a = scene.clear_bgra
+        fb.clearColor(r, g, b, a)
+        fb.clearDepth()
+    cam = (Camera.from_workload(scene.camera) if view_proj is None
+           else Camera.from_matrices(view_proj, scene.camera.position, scene.camera.viewport))
+    pipe = TiledPipeline(ctx, cam, fb)
+    sh = scene.shader
+    pipe.setShader(Shader(sh.kind, tuple(sh.light_direction), tuple(sh.light_color)))
+    pipe.drawMesh(scene.model, m)
+    out = fb.read()
+    ctx.sync()
+    return out

@@ -1,0 +1,824 @@
+// C ABI implementation (include/axr.h): contexts, device resources, per-draw uniforms
+// and launch orchestration. The draw kernels are in kernels.cu; this file only plans
+// and enqueues work on the context's stream.
+#include "axr.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "device_types.h"
+#include "hostmath.h"
+#include "kernels.h"
+
+using namespace axr;
+
+struct axr_texture {
+    uint32_t* texels = nullptr;
+    int32_t width = 0, height = 0;
+    int device = 0;
+};
+
+struct axr_mesh {
+    float4* pos = nullptr;
+    float4* nrm = nullptr;
+    float4* tan = nullptr;
+    float4* bit = nullptr;
+    float2* uv = nullptr;
+    uint32_t* idx = nullptr;
+    DevGroup* groups = nullptr;
+    DevMaterial* materials = nullptr;
+    float* staging = nullptr;  // packed float3 upload area for updates
+    uint32_t num_vertices = 0, num_faces = 0, num_groups = 0, num_materials = 0, num_drawn = 0;
+    int device = 0;
+};
+
+struct axr_framebuffer {
+    uint32_t* color = nullptr;
+    float* depth = nullptr;
+    unsigned long long* key = nullptr;
+    uint32_t* tile_flag = nullptr;
+    uint32_t* tile_queue = nullptr;
+    int32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
+    int device = 0;
+};
+
+struct axr_graph {
+    cudaGraphExec_t exec = nullptr;
+    int device = 0;
+};
+
+struct axr_context {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    LaunchConfig cfg{};
+    std::mutex mu;
+    std::string error;
+    bool capturing = false;
+    // pipeline state (Pipeline::m_Shader, m_Camera, m_Framebuffer)
+    bool has_shader = false, has_camera = false;
+    axr_shader_desc shader{};
+    axr_camera_desc camera{};
+    axr_framebuffer* fb = nullptr;
+    // device scratch arena
+    DevCounters* counters = nullptr;
+    LargeTri* large = nullptr;
+    uint32_t* large_next = nullptr;
+    uint32_t large_cap = 0;
+    int collect_stats = 0;
+    int small_max_pixels = 16;
+    // profiling: per-draw stage events (4 per draw), reused across reads
+    bool profile = false;
+    std::vector<cudaEvent_t> event_pool;
+    size_t events_used = 0;
+    uint64_t launches = 0;
+};
+
+namespace {
+
+thread_local std::string g_no_ctx_error;
+
+axr_status fail(axr_context* ctx, axr_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx)
+        ctx->error = buf;
+    else
+        g_no_ctx_error = buf;
+    return st;
+}
+
+axr_status cuda_fail(axr_context* ctx, cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(ctx, AXR_E_OOM, "%s: out of device memory", what);
+    }
+    return fail(ctx, AXR_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define AXR_CUDA(ctx, call)                                           \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);    \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <class T>
+cudaError_t dmalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+void dfree(void* p) {
+    if (p) cudaFree(p);
+}
+
+DevTexture dev_texture(const axr_texture* t) {
+    DevTexture d{};
+    if (t) {
+        d.texels = t->texels;
+        d.width = t->width;
+        d.height = t->height;
+    }
+    return d;
+}
+
+axr_status grow_scratch(axr_context* ctx, uint32_t faces) {
+    // every face yields at most 8 triangles after clipping; the kernels fall back to
+    // per-thread rasterisation when the list is full, so this bound is a capacity
+    // choice, not a correctness requirement.
+    uint64_t want64 = std::max<uint64_t>(65536, (uint64_t)faces * 2);
+    uint32_t want = (uint32_t)std::min<uint64_t>(want64, 1u << 26);
+    if (want <= ctx->large_cap) return AXR_OK;
+    if (ctx->capturing)
+        return fail(ctx, AXR_E_CAPACITY, "scratch for %u faces not reserved before graph capture", faces);
+    AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->large);
+    dfree(ctx->large_next);
+    ctx->large = nullptr;
+    ctx->large_next = nullptr;
+    ctx->large_cap = 0;
+    AXR_CUDA(ctx, dmalloc(&ctx->large, want));
+    AXR_CUDA(ctx, dmalloc(&ctx->large_next, want));
+    ctx->large_cap = want;
+    return AXR_OK;
+}
+
+axr_status check_mesh_desc(axr_context* ctx, const axr_mesh_desc* d) {
+    if (!d) return fail(ctx, AXR_E_INVALID, "mesh descriptor is NULL");
+    if (d->num_vertices && (!d->positions || !d->uvs || !d->normals))
+        return fail(ctx, AXR_E_INVALID, "mesh needs positions, uvs and normals");
+    if (d->num_faces && !d->indices) return fail(ctx, AXR_E_INVALID, "mesh has faces but no indices");
+    if (d->num_groups && !d->groups) return fail(ctx, AXR_E_INVALID, "mesh has groups but no group array");
+    if (d->num_materials && !d->materials) return fail(ctx, AXR_E_INVALID, "mesh has materials but no array");
+    uint64_t drawn = 0;
+    for (uint32_t g = 0; g < d->num_groups; ++g) {
+        const axr_group_desc& gr = d->groups[g];
+        if ((uint64_t)gr.start_face + gr.face_count > d->num_faces)
+            return fail(ctx, AXR_E_INVALID, "group %u covers faces beyond the mesh", g);
+        if (gr.material >= d->num_materials)
+            return fail(ctx, AXR_E_INVALID, "group %u names material %u of %u", g, gr.material, d->num_materials);
+        drawn += gr.face_count;
+    }
+    if (drawn > kMaxOrdinal + 1ull)
+        return fail(ctx, AXR_E_CAPACITY, "a draw is limited to %u faces", kMaxOrdinal + 1u);
+    for (uint64_t i = 0; i < 3ull * d->num_faces; ++i)
+        if (d->indices[i] >= d->num_vertices)
+            return fail(ctx, AXR_E_INVALID, "face %llu indexes vertex %u of %u", (unsigned long long)(i / 3),
+                        d->indices[i], d->num_vertices);
+    return AXR_OK;
+}
+
+// Upload float3 arrays via the staging buffer and widen them to float4.
+axr_status upload_vec3(axr_context* ctx, axr_mesh* m, const float* src, float4* dst) {
+    if (!src || !dst || m->num_vertices == 0) return AXR_OK;
+    AXR_CUDA(ctx, cudaMemcpyAsync(m->staging, src, 12ull * m->num_vertices, cudaMemcpyHostToDevice, ctx->stream));
+    AXR_CUDA(ctx, launch_pack3(m->staging, dst, m->num_vertices, ctx->stream));
+    ++ctx->launches;
+    return AXR_OK;
+}
+
+axr_status upload_mesh_arrays(axr_context* ctx, axr_mesh* m, const axr_mesh_desc* d) {
+    axr_status st;
+    if ((st = upload_vec3(ctx, m, d->positions, m->pos)) != AXR_OK) return st;
+    if ((st = upload_vec3(ctx, m, d->normals, m->nrm)) != AXR_OK) return st;
+    if ((st = upload_vec3(ctx, m, d->tangents, m->tan)) != AXR_OK) return st;
+    if ((st = upload_vec3(ctx, m, d->bitangents, m->bit)) != AXR_OK) return st;
+    if (m->num_vertices)
+        AXR_CUDA(ctx, cudaMemcpyAsync(m->uv, d->uvs, 8ull * m->num_vertices, cudaMemcpyHostToDevice, ctx->stream));
+    if (m->num_faces)
+        AXR_CUDA(ctx, cudaMemcpyAsync(m->idx, d->indices, 12ull * m->num_faces, cudaMemcpyHostToDevice, ctx->stream));
+    return AXR_OK;
+}
+
+void free_mesh(axr_mesh* m) {
+    if (!m) return;
+    dfree(m->pos); dfree(m->nrm); dfree(m->tan); dfree(m->bit); dfree(m->uv); dfree(m->idx);
+    dfree(m->groups); dfree(m->materials); dfree(m->staging);
+    delete m;
+}
+
+DevUniforms make_uniforms(const axr_camera_desc& cam, const axr_shader_desc& sh, const float* model) {
+    DevUniforms u{};
+    host::M4 vp = host::load(cam.view_proj);
+    host::M4 mm = host::load(model);
+    host::M4 mvp = host::mul(vp, mm);  // viewProj * modelMatrix (src/tiled_pipeline.cpp:149)
+    std::memcpy(u.mvp, mvp.m, sizeof(u.mvp));
+    std::memcpy(u.model, model, sizeof(u.model));
+    if (sh.kind == AXR_SHADER_FLAT) host::normal_matrix(mm, u.normal_mat);
+    std::memcpy(u.cam_pos, cam.position, sizeof(u.cam_pos));
+    std::memcpy(u.light_dir, sh.light_direction, sizeof(u.light_dir));
+    std::memcpy(u.light_color, sh.light_color, sizeof(u.light_color));
+    u.shader = sh.kind;
+    return u;
+}
+
+DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffer* fb, const DevUniforms& u) {
+    DrawParams p{};
+    p.mesh = DevMesh{m->pos, m->nrm, m->tan, m->bit, m->uv, m->idx, m->groups, m->materials,
+                     m->num_vertices, m->num_faces, m->num_groups, m->num_drawn};
+    p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
+                         fb->width, fb->height, fb->tiles_x, fb->tiles_y};
+    p.u = u;
+    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->large_next, ctx->large_cap, ctx->collect_stats};
+    p.small_max_pixels = ctx->small_max_pixels;
+    return p;
+}
+
+bool valid_kind(int32_t k) { return k >= AXR_SHADER_FLAT && k <= AXR_SHADER_GOURAUD; }
+
+}  // namespace
+
+extern "C" {
+
+axr_status axr_context_create(int32_t device, axr_context** out) {
+    if (!out) return fail(nullptr, AXR_E_INVALID, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(nullptr, AXR_E_UNSUPPORTED, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) return fail(nullptr, AXR_E_INVALID, "device %d of %d", device, n);
+    DeviceGuard g(device);
+    auto* ctx = new axr_context();
+    ctx->device = device;
+    cudaDeviceProp prop{};
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e == cudaSuccess && prop.major < 10) {
+        delete ctx;
+        return fail(nullptr, AXR_E_UNSUPPORTED, "device %d is sm_%d%d; this build targets sm_103a", device,
+                    prop.major, prop.minor);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, sizeof(DevCounters));
+    if (e != cudaSuccess) {
+        axr_status st = cuda_fail(nullptr, e, "context setup");
+        if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+        dfree(ctx->counters);
+        delete ctx;
+        return st;
+    }
+    ctx->stream = ctx->own_stream;
+    ctx->cfg.num_sms = prop.multiProcessorCount;
+    ctx->cfg.large_ctas_per_sm = 2;
+    ctx->cfg.resolve_ctas_per_sm = 4;
+    *out = ctx;
+    return AXR_OK;
+}
+
+void axr_context_destroy(axr_context* ctx) {
+    if (!ctx) return;
+    DeviceGuard g(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
+    dfree(ctx->counters);
+    dfree(ctx->large);
+    dfree(ctx->large_next);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+const char* axr_last_error(const axr_context* ctx) { return ctx ? ctx->error.c_str() : g_no_ctx_error.c_str(); }
+
+void* axr_context_stream(axr_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+axr_status axr_context_set_stream(axr_context* ctx, void* stream) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return AXR_OK;
+}
+
+axr_status axr_sync(axr_context* ctx) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t err = 0;
+    AXR_CUDA(ctx, cudaMemcpy(&err, &ctx->counters->error, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) {
+        AXR_CUDA(ctx, cudaMemset(&ctx->counters->error, 0, sizeof(uint32_t)));
+        return fail(ctx, AXR_E_CAPACITY, "device reported error bits 0x%x", err);
+    }
+    return AXR_OK;
+}
+
+axr_status axr_reserve(axr_context* ctx, uint32_t max_faces) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    return grow_scratch(ctx, max_faces);
+}
+
+void* axr_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void axr_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+// ---------------------------------------------------------------- textures
+axr_status axr_texture_create(axr_context* ctx, const uint8_t* rgba, int32_t width, int32_t height,
+                              axr_texture** out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    *out = nullptr;
+    if (width <= 0 || height <= 0 || !rgba) return fail(ctx, AXR_E_INVALID, "texture %dx%d", width, height);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    auto* t = new axr_texture();
+    t->width = width;
+    t->height = height;
+    t->device = ctx->device;
+    size_t n = (size_t)width * (size_t)height;
+    cudaError_t e = dmalloc(&t->texels, n);
+    if (e == cudaSuccess) e = cudaMemcpy(t->texels, rgba, n * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        dfree(t->texels);
+        delete t;
+        return cuda_fail(ctx, e, "texture upload");
+    }
+    *out = t;
+    return AXR_OK;
+}
+
+axr_status axr_texture_update(axr_context* ctx, axr_texture* t, const uint8_t* rgba) {
+    if (!ctx || !t || !rgba) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaMemcpyAsync(t->texels, rgba, (size_t)t->width * t->height * 4, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    return AXR_OK;
+}
+
+void axr_texture_destroy(axr_context* ctx, axr_texture* t) {
+    if (!t) return;
+    DeviceGuard g(t->device);
+    if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+    dfree(t->texels);
+    delete t;
+}
+
+// ---------------------------------------------------------------- meshes
+axr_status axr_mesh_create(axr_context* ctx, const axr_mesh_desc* d, axr_mesh** out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    *out = nullptr;
+    axr_status st = check_mesh_desc(ctx, d);
+    if (st != AXR_OK) return st;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    auto* m = new axr_mesh();
+    m->device = ctx->device;
+    m->num_vertices = d->num_vertices;
+    m->num_faces = d->num_faces;
+    m->num_groups = d->num_groups;
+    m->num_materials = d->num_materials;
+    const uint32_t V = d->num_vertices;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](auto** p, size_t n) {
+        if (e == cudaSuccess) e = dmalloc(p, n);
+    };
+    alloc(&m->pos, V);
+    alloc(&m->nrm, V);
+    alloc(&m->uv, V);
+    if (d->tangents) alloc(&m->tan, V);
+    if (d->bitangents) alloc(&m->bit, V);
+    alloc(&m->idx, 3ull * d->num_faces);
+    alloc(&m->staging, 3ull * V);
+    alloc(&m->groups, std::max<uint32_t>(1, d->num_groups));
+    alloc(&m->materials, std::max<uint32_t>(1, d->num_materials));
+    if (e != cudaSuccess) {
+        free_mesh(m);
+        return cuda_fail(ctx, e, "mesh allocation");
+    }
+    std::vector<DevGroup> groups(std::max<uint32_t>(1, d->num_groups));
+    uint32_t base = 0;
+    for (uint32_t k = 0; k < d->num_groups; ++k) {
+        groups[k] = DevGroup{d->groups[k].start_face, d->groups[k].face_count, base, d->groups[k].material};
+        base += d->groups[k].face_count;
+    }
+    m->num_drawn = base;
+    std::vector<DevMaterial> mats(std::max<uint32_t>(1, d->num_materials));
+    for (uint32_t k = 0; k < d->num_materials; ++k) {
+        const axr_material_desc& md = d->materials[k];
+        DevMaterial& dm = mats[k];
+        dm = DevMaterial{};
+        dm.diffuse = dev_texture(md.diffuse);
+        dm.bump = dev_texture(md.bump);
+        dm.metallic = dev_texture(md.metallic);
+        dm.roughness = dev_texture(md.roughness);
+        dm.ao = dev_texture(md.ao);
+        dm.specular_exponent = md.specular_exponent;
+    }
+    st = upload_mesh_arrays(ctx, m, d);
+    if (st == AXR_OK) {
+        e = cudaMemcpyAsync(m->groups, groups.data(), groups.size() * sizeof(DevGroup), cudaMemcpyHostToDevice,
+                            ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(m->materials, mats.data(), mats.size() * sizeof(DevMaterial),
+                                cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "mesh upload");
+    }
+    if (st != AXR_OK) {
+        free_mesh(m);
+        return st;
+    }
+    *out = m;
+    return AXR_OK;
+}
+
+axr_status axr_mesh_update(axr_context* ctx, axr_mesh* m, const axr_mesh_desc* d) {
+    if (!ctx || !m || !d) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    if (d->num_vertices != m->num_vertices || d->num_faces != m->num_faces)
+        return fail(ctx, AXR_E_INVALID, "mesh update must keep vertex and face counts");
+    if ((d->tangents && !m->tan) || (d->bitangents && !m->bit))
+        return fail(ctx, AXR_E_INVALID, "mesh was created without tangents/bitangents");
+    if (d->num_vertices && (!d->positions || !d->uvs || !d->normals))
+        return fail(ctx, AXR_E_INVALID, "mesh update needs positions, uvs and normals");
+    if (d->num_faces && !d->indices) return fail(ctx, AXR_E_INVALID, "mesh update needs indices");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    return upload_mesh_arrays(ctx, m, d);
+}
+
+void axr_mesh_destroy(axr_context* ctx, axr_mesh* m) {
+    if (!m) return;
+    DeviceGuard g(m->device);
+    if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_mesh(m);
+}
+
+// ---------------------------------------------------------------- framebuffers
+axr_status axr_framebuffer_create(axr_context* ctx, int32_t width, int32_t height, axr_framebuffer** out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    *out = nullptr;
+    if (width <= 0 || height <= 0 || width > 32768 || height > 32768)
+        return fail(ctx, AXR_E_INVALID, "framebuffer %dx%d (1..32768 per side)", width, height);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    auto* fb = new axr_framebuffer();
+    fb->width = width;
+    fb->height = height;
+    fb->tiles_x = (width + kTile - 1) / kTile;
+    fb->tiles_y = (height + kTile - 1) / kTile;
+    fb->device = ctx->device;
+    size_t n = (size_t)width * height, nt = (size_t)fb->tiles_x * fb->tiles_y;
+    cudaError_t e = dmalloc(&fb->color, n);
+    if (e == cudaSuccess) e = dmalloc(&fb->depth, n);
+    if (e == cudaSuccess) e = dmalloc(&fb->key, n);
+    if (e == cudaSuccess) e = dmalloc(&fb->tile_flag, nt);
+    if (e == cudaSuccess) e = dmalloc(&fb->tile_queue, nt);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fb->tile_flag, 0, nt * 4, ctx->stream);
+    if (e == cudaSuccess) e = launch_fill_u64(fb->key, n, kEmptyKey, ctx->stream);
+    // Framebuffer(w, h, true): colour 0, depth +inf (src/framebuffer.cpp:6-14)
+    if (e == cudaSuccess) e = launch_clear(fb->color, fb->depth, n, 0u, INFINITY, true, true, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        dfree(fb->color); dfree(fb->depth); dfree(fb->key); dfree(fb->tile_flag); dfree(fb->tile_queue);
+        delete fb;
+        return cuda_fail(ctx, e, "framebuffer allocation");
+    }
+    *out = fb;
+    return AXR_OK;
+}
+
+void axr_framebuffer_destroy(axr_context* ctx, axr_framebuffer* fb) {
+    if (!fb) return;
+    DeviceGuard g(fb->device);
+    if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx && ctx->fb == fb) ctx->fb = nullptr;
+    dfree(fb->color); dfree(fb->depth); dfree(fb->key); dfree(fb->tile_flag); dfree(fb->tile_queue);
+    delete fb;
+}
+
+axr_status axr_framebuffer_clear_color(axr_context* ctx, axr_framebuffer* fb, uint8_t r, uint8_t g_, uint8_t b,
+                                       uint8_t a) {
+    if (!ctx || !fb) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    // packed a<<24 | r<<16 | g<<8 | b, i.e. bytes B, G, R, A (src/framebuffer.cpp:26-36)
+    uint32_t packed = ((uint32_t)a << 24) | ((uint32_t)r << 16) | ((uint32_t)g_ << 8) | (uint32_t)b;
+    AXR_CUDA(ctx, launch_clear(fb->color, nullptr, (size_t)fb->width * fb->height, packed, 0.f, true, false,
+                               ctx->stream));
+    ++ctx->launches;
+    return AXR_OK;
+}
+
+axr_status axr_framebuffer_clear_depth(axr_context* ctx, axr_framebuffer* fb, float depth) {
+    if (!ctx || !fb) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, launch_clear(nullptr, fb->depth, (size_t)fb->width * fb->height, 0u, depth, false, true,
+                               ctx->stream));
+    ++ctx->launches;
+    return AXR_OK;
+}
+
+static axr_status fb_read(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth, bool wait) {
+    if (!ctx || !fb) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    size_t n = (size_t)fb->width * fb->height;
+    if (bgra) AXR_CUDA(ctx, cudaMemcpyAsync(bgra, fb->color, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (depth) AXR_CUDA(ctx, cudaMemcpyAsync(depth, fb->depth, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (wait) AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return AXR_OK;
+}
+
+axr_status axr_framebuffer_read(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth) {
+    return fb_read(ctx, fb, bgra, depth, true);
+}
+
+axr_status axr_framebuffer_read_async(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth) {
+    return fb_read(ctx, fb, bgra, depth, false);
+}
+
+axr_status axr_framebuffer_write(axr_context* ctx, axr_framebuffer* fb, const uint8_t* bgra, const float* depth) {
+    if (!ctx || !fb) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    size_t n = (size_t)fb->width * fb->height;
+    if (bgra) AXR_CUDA(ctx, cudaMemcpyAsync(fb->color, bgra, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    if (depth) AXR_CUDA(ctx, cudaMemcpyAsync(fb->depth, depth, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return AXR_OK;
+}
+
+axr_status axr_framebuffer_size(const axr_framebuffer* fb, int32_t* width, int32_t* height) {
+    if (!fb) return fail(nullptr, AXR_E_INVALID, "framebuffer is NULL");
+    if (width) *width = fb->width;
+    if (height) *height = fb->height;
+    return AXR_OK;
+}
+
+axr_status axr_framebuffer_device_pointers(const axr_framebuffer* fb, void** bgra, void** depth) {
+    if (!fb) return fail(nullptr, AXR_E_INVALID, "framebuffer is NULL");
+    if (bgra) *bgra = fb->color;
+    if (depth) *depth = fb->depth;
+    return AXR_OK;
+}
+
+// ---------------------------------------------------------------- pipeline state and draws
+axr_status axr_set_shader(axr_context* ctx, const axr_shader_desc* s) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!s) {
+        ctx->has_shader = false;
+        return AXR_OK;
+    }
+    if (!valid_kind(s->kind)) return fail(ctx, AXR_E_INVALID, "unknown shader kind %d", s->kind);
+    ctx->shader = *s;
+    ctx->has_shader = true;
+    return AXR_OK;
+}
+
+axr_status axr_set_camera(axr_context* ctx, const axr_camera_desc* c) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!c) {
+        ctx->has_camera = false;
+        return AXR_OK;
+    }
+    ctx->camera = *c;
+    ctx->has_camera = true;
+    return AXR_OK;
+}
+
+axr_status axr_set_framebuffer(axr_context* ctx, axr_framebuffer* fb) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->fb = fb;
+    return AXR_OK;
+}
+
+axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float model[16]) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    if (!mesh || !model) return fail(ctx, AXR_E_INVALID, "NULL mesh or model matrix");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->has_shader || !ctx->has_camera || !ctx->fb) return AXR_OK;  // src/tiled_pipeline.cpp:146
+    DeviceGuard g(ctx->device);
+    axr_status st = grow_scratch(ctx, mesh->num_drawn);
+    if (st != AXR_OK) return st;
+    DevUniforms u = make_uniforms(ctx->camera, ctx->shader, model);
+    DrawParams p = make_params(ctx, mesh, ctx->fb, u);
+    cudaEvent_t* ev = nullptr;
+    if (ctx->profile && !ctx->capturing) {
+        while (ctx->event_pool.size() < ctx->events_used + 4) {
+            cudaEvent_t e;
+            AXR_CUDA(ctx, cudaEventCreate(&e));
+            ctx->event_pool.push_back(e);
+        }
+        ev = &ctx->event_pool[ctx->events_used];
+        ctx->events_used += 4;
+    }
+    AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, ev, &ctx->launches));
+    return AXR_OK;
+}
+
+axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    if (count < 0 || (count > 0 && !draws)) return fail(ctx, AXR_E_INVALID, "bad draw list");
+    return fail(ctx, AXR_E_UNSUPPORTED, "batched draws are not available in this build");
+}
+
+// ---------------------------------------------------------------- graphs
+axr_status axr_graph_begin(axr_context* ctx) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->capturing) return fail(ctx, AXR_E_INVALID, "capture already active");
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = true;
+    return AXR_OK;
+}
+
+axr_status axr_graph_end(axr_context* ctx, axr_graph** out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->capturing) return fail(ctx, AXR_E_INVALID, "no capture active");
+    DeviceGuard g(ctx->device);
+    ctx->capturing = false;
+    cudaGraph_t graph = nullptr;
+    AXR_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &graph));
+    auto* gr = new axr_graph();
+    gr->device = ctx->device;
+    cudaError_t e = cudaGraphInstantiate(&gr->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        delete gr;
+        return cuda_fail(ctx, e, "graph instantiate");
+    }
+    *out = gr;
+    return AXR_OK;
+}
+
+axr_status axr_graph_launch(axr_context* ctx, axr_graph* gr) {
+    if (!ctx || !gr) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaGraphLaunch(gr->exec, ctx->stream));
+    return AXR_OK;
+}
+
+void axr_graph_destroy(axr_graph* gr) {
+    if (!gr) return;
+    DeviceGuard g(gr->device);
+    if (gr->exec) cudaGraphExecDestroy(gr->exec);
+    delete gr;
+}
+
+// ---------------------------------------------------------------- camera helpers
+axr_status axr_camera_matrices(const float position[3], const float target[3], float fov_degrees, float aspect,
+                               float view[16], float projection[16], float view_proj[16]) {
+    if (!position || !target) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    host::M4 v, p, vp;
+    host::camera_matrices(position, target, fov_degrees, aspect, v, p, vp);
+    if (view) std::memcpy(view, v.m, sizeof(v.m));
+    if (projection) std::memcpy(projection, p.m, sizeof(p.m));
+    if (view_proj) std::memcpy(view_proj, vp.m, sizeof(vp.m));
+    return AXR_OK;
+}
+
+axr_status axr_viewport_matrix(int32_t x, int32_t y, int32_t width, int32_t height, float out[16]) {
+    if (!out) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    host::M4 v = host::viewport_matrix(x, y, width, height);
+    std::memcpy(out, v.m, sizeof(v.m));
+    return AXR_OK;
+}
+
+// ---------------------------------------------------------------- statistics
+axr_status axr_stats_enable(axr_context* ctx, int32_t enable) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->collect_stats = enable ? 1 : 0;
+    return AXR_OK;
+}
+
+axr_status axr_stats_read(axr_context* ctx, axr_draw_stats* out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    DevCounters c{};
+    AXR_CUDA(ctx, cudaMemcpy(&c, ctx->counters, sizeof(c), cudaMemcpyDeviceToHost));
+    out->triangles = c.stat_triangles;
+    out->fragments = c.stat_fragments;
+    out->large = c.stat_large;
+    out->tiles = c.stat_tiles;
+    AXR_CUDA(ctx, cudaMemset(&ctx->counters->stat_triangles, 0, 4 * sizeof(unsigned long long)));
+    return AXR_OK;
+}
+
+// ---------------------------------------------------------------- profiling
+axr_status axr_profile_enable(axr_context* ctx, int32_t enable) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->profile = enable != 0;
+    return AXR_OK;
+}
+
+axr_status axr_profile_read(axr_context* ctx, axr_profile* out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    axr_profile r{};
+    for (size_t k = 0; k + 3 < ctx->events_used; k += 4) {
+        float a = 0, b = 0, c = 0;
+        AXR_CUDA(ctx, cudaEventElapsedTime(&a, ctx->event_pool[k], ctx->event_pool[k + 1]));
+        AXR_CUDA(ctx, cudaEventElapsedTime(&b, ctx->event_pool[k + 1], ctx->event_pool[k + 2]));
+        AXR_CUDA(ctx, cudaEventElapsedTime(&c, ctx->event_pool[k + 2], ctx->event_pool[k + 3]));
+        r.geometry_ms += a;
+        r.large_ms += b;
+        r.resolve_ms += c;
+        ++r.draws;
+    }
+    ctx->events_used = 0;
+    r.kernel_launches = ctx->launches;
+    *out = r;
+    return AXR_OK;
+}
+
+// ---------------------------------------------------------------- stage access
+axr_status axr_debug_triangles(axr_context* ctx, const axr_mesh* mesh, const float model[16],
+                               const float view_proj[16], int32_t width, int32_t height, float* out,
+                               uint32_t capacity, uint32_t* count) {
+    if (!ctx || !mesh || !model || !view_proj || !count) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    if (width <= 0 || height <= 0) return fail(ctx, AXR_E_INVALID, "target %dx%d", width, height);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    axr_camera_desc cam{};
+    std::memcpy(cam.view_proj, view_proj, sizeof(cam.view_proj));
+    axr_shader_desc sh{};
+    sh.kind = AXR_SHADER_GOURAUD;
+    DevUniforms u = make_uniforms(cam, sh, model);
+    axr_framebuffer fake{};
+    fake.width = width;
+    fake.height = height;
+    DrawParams p = make_params(ctx, mesh, &fake, u);
+    float* d_out = nullptr;
+    uint32_t* d_count = nullptr;
+    cudaError_t e = dmalloc(&d_out, 14ull * std::max<uint32_t>(1, capacity));
+    if (e == cudaSuccess) e = dmalloc(&d_count, 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_count, 0, 4, ctx->stream);
+    if (e == cudaSuccess) e = launch_debug_triangles(p, d_out, d_count, capacity, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(count, d_count, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess && out)
+        e = cudaMemcpy(out, d_out, 14ull * 4 * std::min(*count, capacity), cudaMemcpyDeviceToHost);
+    dfree(d_out);
+    dfree(d_count);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "debug triangles");
+    return AXR_OK;
+}
+
+axr_status axr_debug_sample(axr_context* ctx, const axr_texture* tex, const float* uv, int32_t n, float* out) {
+    if (!ctx || !tex || !uv || !out || n < 0) return fail(ctx, AXR_E_INVALID, "bad argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    float2* d_uv = nullptr;
+    float4* d_out = nullptr;
+    cudaError_t e = dmalloc(&d_uv, std::max(1, n));
+    if (e == cudaSuccess) e = dmalloc(&d_out, std::max(1, n));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_uv, uv, 8ull * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = launch_debug_sample(dev_texture(tex), d_uv, d_out, (uint32_t)n, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, 16ull * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dfree(d_uv);
+    dfree(d_out);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "debug sample");
+    return AXR_OK;
+}
+
+}  // extern "C"

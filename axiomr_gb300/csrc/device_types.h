@@ -1,0 +1,125 @@
+// Data layout in device memory (HBM), shared by the host code and the kernels.
+//
+// Mesh (SoA, one array per attribute, reference include/mesh.hpp:9-18):
+//   pos[V]   float4 (x, y, z, 0)   one 16-byte load per vertex gather
+//   nrm[V]   float4                 tan[V], bit[V] float4 (optional, NULL reads as 0)
+//   uv[V]    float2
+//   idx[3F]  uint32                 Face::vertexIndices, 3 per face
+//   groups   DevGroup[G]            MaterialGroup (start face, count, material) + the
+//                                   group's first position in draw order
+// Texture: RGBA8 texels, row 0 first (as stbi_load returns them), one uint32 per texel.
+// Framebuffer: color[W*H] uint32 holding B,G,R,A bytes (row 0 = bottom, reference
+//   include/framebuffer.hpp:14-21), depth[W*H] float, key[W*H] uint64 (depth|order
+//   visibility keys, all-ones between draws), tile_flag[TX*TY] uint32, tile_queue[TX*TY].
+#pragma once
+#include <stdint.h>
+#include <vector_types.h>
+
+namespace axr {
+
+constexpr int kTile = 16;            // reference TILE_SIZE (include/tiled_pipeline.hpp:28)
+constexpr int kMaxClipVerts = 24;    // reference MAX_CLIPPED_VERTS (include/pipeline.hpp:17)
+constexpr uint32_t kMaxOrdinal = (1u << 28) - 1;  // faces per draw: tag = ordinal*16 + clip bits
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;  // no triangle covers the pixel yet
+
+enum ShaderKind : int32_t { kFlat = 0, kPhong = 1, kPBR = 2, kBlinnPhong = 3, kGouraud = 4 };
+
+struct DevTexture {
+    const uint32_t* texels;
+    int32_t width, height;
+};
+
+struct DevMaterial {
+    DevTexture diffuse, bump, metallic, roughness, ao;
+    float specular_exponent;
+    float pad_[3];
+};
+
+struct DevGroup {
+    uint32_t start;     // first face index
+    uint32_t count;     // faces
+    uint32_t base;      // position of the first face in draw order
+    uint32_t material;  // index into the material table
+};
+
+struct DevMesh {
+    const float4* pos;
+    const float4* nrm;
+    const float4* tan;
+    const float4* bit;
+    const float2* uv;
+    const uint32_t* idx;
+    const DevGroup* groups;
+    const DevMaterial* materials;
+    uint32_t num_vertices, num_faces, num_groups, num_drawn;
+};
+
+struct DevTarget {
+    uint32_t* color;
+    float* depth;
+    unsigned long long* key;
+    uint32_t* tile_flag;
+    uint32_t* tile_queue;
+    int32_t width, height, tiles_x, tiles_y;
+};
+
+// Per-draw uniforms (reference include/IShader.hpp:39-45 and the shaders' light fields).
+struct DevUniforms {
+    float mvp[16];       // viewProj * model, column-major
+    float model[16];
+    float normal_mat[9]; // mat3(transpose(inverse(model))), FlatShader
+    float cam_pos[3];
+    float light_dir[3];
+    float light_color[3];
+    int32_t shader;
+    int32_t pad_;
+};
+
+// A triangle too large for the per-thread rasteriser: its setup is stored once and its
+// 16x16 tiles are handed out to warps (64 bytes, one per triangle).
+struct LargeTri {
+    float e[9];          // edge a, b, c for edges 0..2 after the area-sign flip
+    float inv_area;
+    float z[3];
+    uint32_t tag;        // ordinal * 16 + clip bits: low word of the depth key
+    uint16_t x_lo, x_hi, y_lo, y_hi;  // covered pixel range [lo, hi), clipped to the target
+};
+
+// Work counters of one draw (all zero between draws; the last CTA of each kernel that
+// consumes a counter resets it).
+struct DevCounters {
+    uint32_t large_count;     // LargeTri entries appended (may exceed capacity: overflow flag)
+    uint32_t large_cursor;    // first entry not yet fully handed out
+    uint32_t large_done;      // CTAs of the large-triangle kernel that finished
+    uint32_t queue_len;       // dirty tiles appended
+    uint32_t queue_head;      // dirty tiles handed out
+    uint32_t resolve_done;    // CTAs of the resolve kernel that finished
+    uint32_t error;           // sticky error bits (kErr*)
+    uint32_t pad_;
+    unsigned long long stat_triangles;   // triangles that passed clip + cull
+    unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
+    unsigned long long stat_large;       // triangles sent to the tile rasteriser
+    unsigned long long stat_tiles;       // dirty tiles resolved
+};
+
+constexpr uint32_t kErrOrdinal = 1u;  // more faces than a depth key can order
+constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh (face skipped)
+
+struct DevScratch {
+    DevCounters* counters;
+    LargeTri* large;
+    uint32_t* large_next;     // per entry: next tile to hand out
+    uint32_t large_cap;
+    int32_t collect_stats;
+};
+
+struct DrawParams {
+    DevMesh mesh;
+    DevTarget target;
+    DevUniforms u;
+    DevScratch scratch;
+    int32_t small_max_pixels;  // triangles whose pixel box is at most this are rasterised per thread
+    int32_t pad_;
+};
+
+}  // namespace axr

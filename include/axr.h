@@ -1,0 +1,264 @@
+/* AxiomR-GB300 C ABI: the AxiomR software-rasterisation draw path on one GB300 GPU.
+ *
+ * This header is the drop-in boundary for AxiomR's renderer draw path. Each entry point
+ * names the reference interface it replaces (paths relative to the AxiomR tree). The
+ * library owns all device memory behind the opaque handles; callers own the handles.
+ * No C++ types, exceptions or CUDA types cross this boundary: streams are passed as
+ * void* (a cudaStream_t), sizes as fixed-width integers.
+ *
+ * Threading: one axr_context per host thread (calls on a context are serialised by an
+ * internal lock). Work is enqueued on the context's CUDA stream in call order;
+ * axr_sync() waits for it. Resources (meshes, textures, framebuffers) may be shared by
+ * contexts on the same device, but a framebuffer must not be drawn by two contexts at
+ * once.
+ *
+ * Results are bit-identical to the reference's CPU pipeline for coverage and depth-test
+ * winners and depth values, and within 1 LSB per 8-bit colour channel.
+ */
+#ifndef AXR_H
+#define AXR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AXR_ABI_VERSION 1
+
+/* The reference reports failures with exceptions or silently (src/tiled_pipeline.cpp:146,
+ * 126; include/thread_pool.hpp:23-24); across a C ABI they become status codes, with a
+ * message available from axr_last_error(). */
+typedef enum axr_status {
+    AXR_OK = 0,
+    AXR_E_INVALID = 1,     /* bad argument or handle */
+    AXR_E_OOM = 2,         /* device or host allocation failed */
+    AXR_E_BUDGET = 3,      /* device-memory budget of the serving loop exceeded */
+    AXR_E_TIMEOUT = 4,     /* a bounded wait gave up */
+    AXR_E_CUDA = 5,        /* CUDA runtime error (see axr_last_error) */
+    AXR_E_UNSUPPORTED = 6, /* no usable GPU / device capability missing */
+    AXR_E_CAPACITY = 7     /* a preset capacity (faces per draw, captured graph) is too small */
+} axr_status;
+
+/* Shader kinds. FLAT, PHONG and PBR are the reference's FlatShader, PhongShader and
+ * PBRShader (include/shaders/shaders.hpp:19-62, 140-247, 252-423). BLINN_PHONG and
+ * GOURAUD are this library's own (the reference has neither): Blinn-Phong follows
+ * PhongShader with the half-vector specular term and no normal map; Gouraud
+ * interpolates a per-vertex RGBA colour carried as RGB in the vertex normal and A in
+ * uv.x (the reference Vertex has no colour field, include/mesh.hpp:9-14). */
+typedef enum axr_shader_kind {
+    AXR_SHADER_FLAT = 0,
+    AXR_SHADER_PHONG = 1,
+    AXR_SHADER_PBR = 2,
+    AXR_SHADER_BLINN_PHONG = 3,
+    AXR_SHADER_GOURAUD = 4
+} axr_shader_kind;
+
+typedef struct axr_context axr_context;
+typedef struct axr_texture axr_texture;
+typedef struct axr_mesh axr_mesh;
+typedef struct axr_framebuffer axr_framebuffer;
+
+/* ------------------------------------------------------------------ context
+ * Replaces TiledPipeline(threads, Camera*, Framebuffer*) and its thread pool and arenas
+ * (include/tiled_pipeline.hpp:58-62, 98-119; src/tiled_pipeline.cpp:123-139): the
+ * context holds the pipeline state, a CUDA stream and the device scratch arena. */
+axr_status axr_context_create(int32_t device, axr_context** out);
+void axr_context_destroy(axr_context* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* axr_last_error(const axr_context* ctx);
+/* The context's cudaStream_t (created non-blocking by axr_context_create). */
+void* axr_context_stream(axr_context* ctx);
+/* Use a caller-owned cudaStream_t instead (NULL restores the context's own stream). */
+axr_status axr_context_set_stream(axr_context* ctx, void* stream);
+/* Wait for all work enqueued on the context's stream; reports device-side errors. */
+axr_status axr_sync(axr_context* ctx);
+/* Pre-size the scratch arena for draws of up to max_faces faces (needed before a draw
+ * is captured into a CUDA graph; draws outside a capture grow it on demand). */
+axr_status axr_reserve(axr_context* ctx, uint32_t max_faces);
+
+/* Pinned (page-locked) host memory for asynchronous uploads and read-backs. */
+void* axr_host_alloc(size_t bytes);
+void axr_host_free(void* p);
+
+/* ------------------------------------------------------------------ textures
+ * Replaces Texture (include/texture.hpp:7-64, src/texture.cpp:21-36): RGBA8 texels,
+ * row 0 first as stbi_load(..., STBI_rgb_alpha) returns them; sampling is the
+ * reference's nearest / clamp-to-edge / y-flipped Texture::sample (texture.hpp:12-34). */
+axr_status axr_texture_create(axr_context* ctx, const uint8_t* rgba, int32_t width, int32_t height,
+                              axr_texture** out);
+/* Replace all texels (same size), asynchronously on the context stream. */
+axr_status axr_texture_update(axr_context* ctx, axr_texture* tex, const uint8_t* rgba);
+void axr_texture_destroy(axr_context* ctx, axr_texture* tex);
+
+/* ------------------------------------------------------------------ meshes
+ * Replaces Mesh / Vertex / Face / MaterialGroup / Material (include/mesh.hpp:9-101).
+ * Vertex attributes are separate arrays (structure of arrays) instead of the reference's
+ * 56-byte interleaved Vertex; indices are 3 per face. A material group draws faces
+ * [start_face, start_face + face_count) with one material; draw order is group order,
+ * then face order inside the group (src/tiled_pipeline.cpp:176-259). */
+typedef struct axr_material_desc {
+    const axr_texture* diffuse;   /* map_Kd */
+    const axr_texture* bump;      /* map_Bump / bump / norm (Phong, PBR) */
+    const axr_texture* metallic;  /* map_Ks / refl (PBR) */
+    const axr_texture* roughness; /* map_Ns (PBR) */
+    const axr_texture* ao;        /* map_A0 (PBR) */
+    float specular_exponent;      /* Ns (Phong, Blinn-Phong use Ns * 50) */
+} axr_material_desc;
+
+typedef struct axr_group_desc {
+    uint32_t start_face;
+    uint32_t face_count;
+    uint32_t material;
+} axr_group_desc;
+
+typedef struct axr_mesh_desc {
+    uint32_t num_vertices;
+    const float* positions;  /* 3 per vertex */
+    const float* uvs;        /* 2 per vertex */
+    const float* normals;    /* 3 per vertex */
+    const float* tangents;   /* 3 per vertex, or NULL (zero) */
+    const float* bitangents; /* 3 per vertex, or NULL (zero) */
+    uint32_t num_faces;
+    const uint32_t* indices; /* 3 per face */
+    uint32_t num_groups;
+    const axr_group_desc* groups;
+    uint32_t num_materials;
+    const axr_material_desc* materials;
+} axr_mesh_desc;
+
+/* Upload a mesh (host pointers; the call returns after the data has been copied). */
+axr_status axr_mesh_create(axr_context* ctx, const axr_mesh_desc* desc, axr_mesh** out);
+/* Re-upload vertex attributes and indices of an existing mesh with the same counts,
+ * asynchronously on the context stream (host buffers must stay valid until then;
+ * pinned memory from axr_host_alloc makes the copies truly asynchronous). */
+axr_status axr_mesh_update(axr_context* ctx, axr_mesh* mesh, const axr_mesh_desc* desc);
+void axr_mesh_destroy(axr_context* ctx, axr_mesh* mesh);
+
+/* ------------------------------------------------------------------ framebuffers
+ * Replaces Framebuffer (include/framebuffer.hpp:9-69, src/framebuffer.cpp:6-42):
+ * colour is 4 bytes per pixel in B, G, R, A order, row 0 at the bottom; depth is one
+ * float per pixel (NDC z, smaller is nearer). Created cleared like the reference's
+ * constructor: colour 0, depth +inf. */
+axr_status axr_framebuffer_create(axr_context* ctx, int32_t width, int32_t height, axr_framebuffer** out);
+void axr_framebuffer_destroy(axr_context* ctx, axr_framebuffer* fb);
+/* Framebuffer::clearColor(Color{r,g,b,a}) (framebuffer.cpp:26-36) */
+axr_status axr_framebuffer_clear_color(axr_context* ctx, axr_framebuffer* fb, uint8_t r, uint8_t g, uint8_t b,
+                                       uint8_t a);
+/* Framebuffer::clearDepth(value) (framebuffer.cpp:38-42; the reference default is +inf) */
+axr_status axr_framebuffer_clear_depth(axr_context* ctx, axr_framebuffer* fb, float depth);
+/* Copy colour (W*H*4 bytes) and/or depth (W*H floats) to host memory; either may be
+ * NULL. Blocks until the data is on the host. */
+axr_status axr_framebuffer_read(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth);
+/* Enqueue the same copies without waiting (use pinned memory and axr_sync). */
+axr_status axr_framebuffer_read_async(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth);
+/* Upload host colour and/or depth into the framebuffer (either may be NULL). */
+axr_status axr_framebuffer_write(axr_context* ctx, axr_framebuffer* fb, const uint8_t* bgra, const float* depth);
+axr_status axr_framebuffer_size(const axr_framebuffer* fb, int32_t* width, int32_t* height);
+/* Device pointers of the colour (uint32 per pixel) and depth planes, for interop. */
+axr_status axr_framebuffer_device_pointers(const axr_framebuffer* fb, void** bgra, void** depth);
+
+/* ------------------------------------------------------------------ pipeline state
+ * Pipeline::setShader / setCamera / setFramebuffer (include/pipeline.hpp:22-24). The
+ * shader object's uniforms become a plain descriptor: the IShader virtuals
+ * (include/IShader.hpp:30-46) cannot cross a C ABI. */
+typedef struct axr_shader_desc {
+    int32_t kind;              /* axr_shader_kind */
+    float light_direction[3];  /* lightDirection (shaders.hpp:60, 244, 402) */
+    float light_color[3];      /* lightColor (shaders.hpp:245, 403) */
+} axr_shader_desc;
+
+/* What drawMesh reads from the Camera (src/tiled_pipeline.cpp:148-155): the
+ * view-projection and viewport matrices (column-major) and the eye position. */
+typedef struct axr_camera_desc {
+    float view_proj[16];
+    float viewport[16];
+    float position[3];
+} axr_camera_desc;
+
+axr_status axr_set_shader(axr_context* ctx, const axr_shader_desc* shader);
+axr_status axr_set_camera(axr_context* ctx, const axr_camera_desc* camera);
+axr_status axr_set_framebuffer(axr_context* ctx, axr_framebuffer* fb);
+
+/* TiledPipeline::drawMesh(modelMatrix, mesh) (include/tiled_pipeline.hpp:62,
+ * src/tiled_pipeline.cpp:143-322), called by Renderer::drawMesh (src/renderer.cpp:16-19).
+ * Enqueued on the context stream. Like the reference, a draw with no shader, camera or
+ * framebuffer set does nothing (src/tiled_pipeline.cpp:146). */
+axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
+
+/* ------------------------------------------------------------------ batched form
+ * Many independent draws (each with its own framebuffer, camera, shader and mesh) in
+ * one persistent launch over a shared work queue; no reference counterpart (the
+ * reference issues one drawMesh per mesh). Framebuffers must be distinct within a
+ * batch. */
+typedef struct axr_draw_desc {
+    const axr_mesh* mesh;
+    axr_framebuffer* framebuffer;
+    float model[16];
+    axr_camera_desc camera;
+    axr_shader_desc shader;
+} axr_draw_desc;
+
+axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count);
+
+/* ------------------------------------------------------------------ CUDA graphs
+ * Record the draws issued on the context between begin and end into a CUDA graph and
+ * replay it. Scratch must be reserved (axr_reserve / axr_batch_reserve) beforehand. */
+typedef struct axr_graph axr_graph;
+axr_status axr_graph_begin(axr_context* ctx);
+axr_status axr_graph_end(axr_context* ctx, axr_graph** out);
+axr_status axr_graph_launch(axr_context* ctx, axr_graph* graph);
+void axr_graph_destroy(axr_graph* graph);
+
+/* ------------------------------------------------------------------ camera helpers
+ * Camera (src/camera.cpp:30-100, 191-205): matrices of a camera at `position` looking
+ * at `target`, vertical field of view in degrees, aspect ratio, near 0.1, far 100, as
+ * Camera(position, target, fov, aspect) followed by update(0). */
+axr_status axr_camera_matrices(const float position[3], const float target[3], float fov_degrees, float aspect,
+                               float view[16], float projection[16], float view_proj[16]);
+axr_status axr_viewport_matrix(int32_t x, int32_t y, int32_t width, int32_t height, float out[16]);
+
+/* ------------------------------------------------------------------ statistics
+ * Counters of the draws issued since the last reset (collection slows the kernels a
+ * little and is off by default). */
+typedef struct axr_draw_stats {
+    uint64_t triangles;  /* triangles that survived clipping and culling */
+    uint64_t fragments;  /* covered (triangle, pixel) pairs */
+    uint64_t large;      /* triangles rasterised by the tile kernel */
+    uint64_t tiles;      /* 16x16 tiles resolved */
+} axr_draw_stats;
+axr_status axr_stats_enable(axr_context* ctx, int32_t enable);
+axr_status axr_stats_read(axr_context* ctx, axr_draw_stats* out); /* synchronises, then resets */
+
+/* ------------------------------------------------------------------ profiling
+ * When enabled, every draw records CUDA events on the context stream between its
+ * kernels; axr_profile_read synchronises and returns the summed device time of each stage
+ * since the last read, and the number of kernels the library launched. */
+typedef struct axr_profile {
+    uint32_t draws;          /* draws recorded */
+    uint32_t pad_;
+    double geometry_ms;      /* transform, clip, cull, setup, small-triangle raster */
+    double large_ms;         /* large-triangle tile raster */
+    double resolve_ms;       /* per-tile resolve and shading */
+    uint64_t kernel_launches;/* all kernels launched on this context since creation */
+} axr_profile;
+axr_status axr_profile_enable(axr_context* ctx, int32_t enable);
+axr_status axr_profile_read(axr_context* ctx, axr_profile* out);
+
+/* ------------------------------------------------------------------ stage access (tests)
+ * Every triangle of a draw that survives clipping and culling, as 14 words each:
+ * tag (uint32: draw-order position * 16 + clip bits), screen x0 y0 x1 y1 x2 y2, NDC z0..z2,
+ * minX, minY, maxX, maxY; unordered. Mirrors the reference's Triangle records
+ * (include/tiled_pipeline.hpp:14-26) produced by the clip stage (src/tiled_pipeline.cpp:185-240).
+ * Writes min(count, capacity) records to `out` (host) and the count to *count. */
+axr_status axr_debug_triangles(axr_context* ctx, const axr_mesh* mesh, const float model[16],
+                               const float view_proj[16], int32_t width, int32_t height, float* out,
+                               uint32_t capacity, uint32_t* count);
+/* Texture::sample at n uv pairs (host arrays) -> n RGBA floats. */
+axr_status axr_debug_sample(axr_context* ctx, const axr_texture* tex, const float* uv, int32_t n, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AXR_H */

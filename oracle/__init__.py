@@ -125,7 +125,9 @@ class Oracle:
         self._shade.argtypes = [vp, vp, fp, fp, fp, fp, fp, fp]
         self._render = getattr(self.lib, p + "render")
         self._render.argtypes = [vp, fp, vp, vp, i32, i32, i32, i32, vp, fp, fp]
-        for f in (self._camera, self._clip, self._tri, self._sample, self._shade, self._render):
+        self._draw = getattr(self.lib, p + "draw")
+        self._draw.argtypes = [vp, fp, fp, fp, vp, i32, i32, i32, vp, fp]
+        for f in (self._camera, self._clip, self._tri, self._sample, self._shade, self._render, self._draw):
             f.restype = C.c_int
 
     # -- stages -----------------------------------------------------------------------
@@ -193,6 +195,28 @@ class Oracle:
         if rc:
             raise RuntimeError(f"{self.kind}_render failed ({rc})")
         return bgra, depth, mats.reshape(3, 16)
+
+
+    def draw(self, scene, view_proj, cam_pos=None, bgra=None, depth=None, threads: int = 0):
+        """Draw `scene` with an explicit view-projection matrix (16 floats, column-major)
+        and eye position (default: the scene camera's). Returns (bgra, depth)."""
+        from axiomr_gb300.workloads import clear_framebuffer
+
+        if bgra is None or depth is None:
+            bgra, depth = clear_framebuffer(scene)
+        bgra = np.ascontiguousarray(bgra, np.uint8).copy()
+        depth = np.ascontiguousarray(depth, np.float32).copy()
+        keep = _Keep()
+        mesh = make_mesh(keep, scene.mesh)
+        sh = make_shader(scene.shader)
+        model = keep.arr(scene.model, np.float32)
+        vp = keep.arr(np.asarray(view_proj, np.float32).reshape(16), np.float32)
+        cp = keep.arr(np.asarray(scene.camera.position if cam_pos is None else cam_pos, np.float32), np.float32)
+        rc = self._draw(C.addressof(mesh), model.ctypes.data, vp.ctypes.data, cp.ctypes.data, C.addressof(sh),
+                        scene.width, scene.height, threads, bgra.ctypes.data, depth.ctypes.data)
+        if rc:
+            raise RuntimeError(f"{self.kind}_draw failed ({rc})")
+        return bgra, depth
 
 
 def ref_available() -> bool:

@@ -55,6 +55,8 @@ int port_triangle(const float* in3, int width, int height, float* out13, int* ba
 int port_sample(const axo_texture* t, const float* uv, int n, float* out);
 int port_shade(const axo_shader* sh, const axo_material* mat, const float* model, const float* view_proj,
                const float* cam_pos, const float* verts, const float* bar, float* out);
+int port_draw(const axo_mesh* mesh, const float* model, const float* view_proj, const float* cam_pos,
+              const axo_shader* shader, int width, int height, int threads, uint8_t* bgra, float* depth);
 int port_render(const axo_mesh* mesh, const float* model, const axo_camera* camera, const axo_shader* shader,
                 int width, int height, int threads, int max_faces_per_draw, uint8_t* bgra, float* depth,
                 float* matrices_out48);

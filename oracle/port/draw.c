@@ -291,10 +291,8 @@ static void raster_task(void* p, int tid, int nthreads) {
 }
 
 /* ------------------------------------------------------------------ draw */
-int port_render(const axo_mesh* mesh, const float* model, const axo_camera* camera, const axo_shader* shader,
-                int width, int height, int threads, int max_faces_per_draw, uint8_t* bgra, float* depth,
-                float* matrices_out48) {
-    (void)max_faces_per_draw; /* no arena limit in the port */
+int port_draw(const axo_mesh* mesh, const float* model, const float* view_proj, const float* cam_pos,
+              const axo_shader* shader, int width, int height, int threads, uint8_t* bgra, float* depth) {
     if (shader->kind < AXO_FLAT || shader->kind > AXO_GOURAUD || width <= 0 || height <= 0) return 1;
     for (uint32_t g = 0; g < mesh->num_groups; ++g) {
         const uint32_t* gr = mesh->groups + 3 * g;
@@ -302,17 +300,9 @@ int port_render(const axo_mesh* mesh, const float* model, const axo_camera* came
     }
     pthread_mutex_lock(&g_render_mu);
     int nthreads = threads > 0 ? threads : hw_threads();
-
-    m4 view, proj, vp;
-    port_camera_matrices(camera, &view, &proj, &vp);
-    if (matrices_out48) {
-        m4_store(&view, matrices_out48);
-        m4_store(&proj, matrices_out48 + 16);
-        m4_store(&vp, matrices_out48 + 32);
-    }
-    m4 M = m4_load(model);
+    m4 M = m4_load(model), vp = m4_load(view_proj);
     shader_state sh;
-    shader_init(&sh, shader, &M, &vp, V3(camera->position[0], camera->position[1], camera->position[2]));
+    shader_init(&sh, shader, &M, &vp, V3(cam_pos[0], cam_pos[1], cam_pos[2]));
 
     /* 1. clip stage, per material group (cpp:176-260) */
     tri_vec all = {0};
@@ -401,4 +391,19 @@ int port_render(const axo_mesh* mesh, const float* model, const axo_camera* came
     free(all.data);
     pthread_mutex_unlock(&g_render_mu);
     return 0;
+}
+
+/* Camera(position, target, fov, aspect) + update(0), then port_draw with its matrices. */
+int port_render(const axo_mesh* mesh, const float* model, const axo_camera* camera, const axo_shader* shader,
+                int width, int height, int threads, int max_faces_per_draw, uint8_t* bgra, float* depth,
+                float* matrices_out48) {
+    (void)max_faces_per_draw; /* the port has no triangle arena limit */
+    m4 view, proj, vp;
+    port_camera_matrices(camera, &view, &proj, &vp);
+    float m[48];
+    m4_store(&view, m);
+    m4_store(&proj, m + 16);
+    m4_store(&vp, m + 32);
+    if (matrices_out48) memcpy(matrices_out48, m, sizeof(m));
+    return port_draw(mesh, model, m + 32, camera->position, shader, width, height, threads, bgra, depth);
 }

@@ -50,6 +50,8 @@ struct TexData { using type = unsigned char* AR::Texture::*; friend type member(
 struct TexWidth { using type = int AR::Texture::*; friend type member(TexWidth); };
 struct TexHeight { using type = int AR::Texture::*; friend type member(TexHeight); };
 struct TexChannels { using type = int AR::Texture::*; friend type member(TexChannels); };
+struct CamViewProj { using type = glm::mat4 AR::Camera::*; friend type member(CamViewProj); };
+struct CamPosition { using type = glm::vec3 AR::Camera::*; friend type member(CamPosition); };
 template struct Expose<MeshVertices, &AR::Mesh::m_Vertices>;
 template struct Expose<MeshFaces, &AR::Mesh::m_Faces>;
 template struct Expose<MeshMaterials, &AR::Mesh::m_Materials>;
@@ -58,6 +60,8 @@ template struct Expose<TexData, &AR::Texture::m_Data>;
 template struct Expose<TexWidth, &AR::Texture::m_Width>;
 template struct Expose<TexHeight, &AR::Texture::m_Height>;
 template struct Expose<TexChannels, &AR::Texture::m_Channels>;
+template struct Expose<CamViewProj, &AR::Camera::m_ViewProjection>;
+template struct Expose<CamPosition, &AR::Camera::m_Position>;
 
 // Pipeline::clipTriangle is protected static (reference include/pipeline.hpp:34-42).
 struct ClipAccess : AR::Pipeline {
@@ -253,6 +257,56 @@ int shade_with(const axo_shader& sh, const axo_material& mat, const float* model
     return 0;
 }
 
+
+// TiledPipeline::drawMesh (reference src/tiled_pipeline.cpp:143-322) into a caller-owned
+// BGRA8 + f32 framebuffer (read and written in place). Each material group is drawn in
+// chunks of at most max_faces_per_draw faces, one single-group drawMesh per chunk: the
+// reference's 16 MiB triangle arena has a null upstream (include/tiled_pipeline.hpp:98-104,
+// src/tiled_pipeline.cpp:126) and throws std::bad_alloc above roughly 35k triangles per
+// draw. Chunked draws in face order give the same image as one draw, because both the
+// per-tile early-Z (cpp:569) and the merge (cpp:1150) are strict less-than.
+// Returns 0 on success, 1 on bad arguments, 2 on a reference exception.
+int draw_with_camera(AR::Camera& cam, const axo_mesh* mesh, const float* model, const axo_shader* shader, int width,
+                     int height, int threads, int max_faces_per_draw, uint8_t* bgra, float* depth) {
+    AR::Framebuffer fb(width, height, true);
+    std::memcpy(fb.getColorData(), bgra, size_t(width) * height * 4);
+    std::memcpy(fb.getDepthData(), depth, size_t(width) * height * 4);
+
+    AR::Mesh m;
+    auto& verts = m.*member(MeshVertices{});
+    auto& faces = m.*member(MeshFaces{});
+    auto& mats = m.*member(MeshMaterials{});
+    auto& groups = m.*member(MeshGroups{});
+    verts.resize(mesh->num_vertices);
+    for (uint32_t i = 0; i < mesh->num_vertices; ++i) verts[i] = vertex_at(*mesh, i);
+    faces.resize(mesh->num_faces);
+    for (uint32_t f = 0; f < mesh->num_faces; ++f)
+        faces[f].vertexIndices = {mesh->indices[3 * f], mesh->indices[3 * f + 1], mesh->indices[3 * f + 2]};
+    for (uint32_t k = 0; k < mesh->num_materials; ++k) {
+        std::string name = "m" + std::to_string(k);
+        mats[name] = make_material(mesh->materials[k], name);
+    }
+
+    auto sh = make_shader(*shader);
+    if (!sh) return 1;
+    size_t nthreads = threads > 0 ? size_t(threads) : std::max<size_t>(1, std::thread::hardware_concurrency());
+    auto pipe = std::make_unique<AR::TiledPipeline>(nthreads, &cam, &fb);
+    pipe->setShader(sh.get());
+    glm::mat4 M = load_mat4(model);
+    size_t chunk = max_faces_per_draw > 0 ? size_t(max_faces_per_draw) : size_t(16384);
+    for (uint32_t g = 0; g < mesh->num_groups; ++g) {
+        size_t start = mesh->groups[3 * g], count = mesh->groups[3 * g + 1];
+        std::string name = "m" + std::to_string(mesh->groups[3 * g + 2]);
+        for (size_t s = 0; s < count; s += chunk) {
+            groups.assign(1, AR::MaterialGroup{name, start + s, std::min(chunk, count - s)});
+            pipe->drawMesh(M, m);
+        }
+    }
+    std::memcpy(bgra, fb.getColorData(), size_t(width) * height * 4);
+    std::memcpy(depth, fb.getDepthData(), size_t(width) * height * 4);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -314,14 +368,7 @@ int ref_shade(const axo_shader* sh, const axo_material* mat, const float* model,
     }
 }
 
-// TiledPipeline::drawMesh (reference src/tiled_pipeline.cpp:143-322) into a caller-owned
-// BGRA8 + f32 framebuffer (read and written in place). Each material group is drawn in
-// chunks of at most max_faces_per_draw faces, one single-group drawMesh per chunk: the
-// reference's 16 MiB triangle arena has a null upstream (include/tiled_pipeline.hpp:98-104,
-// src/tiled_pipeline.cpp:126) and throws std::bad_alloc above roughly 35k triangles per
-// draw. Chunked draws in face order give the same image as one draw, because both the
-// per-tile early-Z (cpp:569) and the merge (cpp:1150) are strict less-than.
-// Returns 0 on success, 2 on a reference exception (e.g. the arena overflow).
+// Camera(position, target, fov, aspect) + update(0), then draw_with_camera.
 int ref_render(const axo_mesh* mesh, const float* model, const axo_camera* camera, const axo_shader* shader,
                int width, int height, int threads, int max_faces_per_draw, uint8_t* bgra, float* depth,
                float* matrices_out48) {
@@ -332,45 +379,27 @@ int ref_render(const axo_mesh* mesh, const float* model, const axo_camera* camer
             store_mat4(cam.getProjectionMatrix(), matrices_out48 + 16);
             store_mat4(cam.getViewProjectionMatrix(), matrices_out48 + 32);
         }
-        AR::Framebuffer fb(width, height, true);
-        std::memcpy(fb.getColorData(), bgra, size_t(width) * height * 4);
-        std::memcpy(fb.getDepthData(), depth, size_t(width) * height * 4);
-
-        AR::Mesh m;
-        auto& verts = m.*member(MeshVertices{});
-        auto& faces = m.*member(MeshFaces{});
-        auto& mats = m.*member(MeshMaterials{});
-        auto& groups = m.*member(MeshGroups{});
-        verts.resize(mesh->num_vertices);
-        for (uint32_t i = 0; i < mesh->num_vertices; ++i) verts[i] = vertex_at(*mesh, i);
-        faces.resize(mesh->num_faces);
-        for (uint32_t f = 0; f < mesh->num_faces; ++f)
-            faces[f].vertexIndices = {mesh->indices[3 * f], mesh->indices[3 * f + 1], mesh->indices[3 * f + 2]};
-        for (uint32_t k = 0; k < mesh->num_materials; ++k) {
-            std::string name = "m" + std::to_string(k);
-            mats[name] = make_material(mesh->materials[k], name);
-        }
-
-        auto sh = make_shader(*shader);
-        if (!sh) return 1;
-        size_t nthreads = threads > 0 ? size_t(threads) : std::max<size_t>(1, std::thread::hardware_concurrency());
-        auto pipe = std::make_unique<AR::TiledPipeline>(nthreads, &cam, &fb);
-        pipe->setShader(sh.get());
-        glm::mat4 M = load_mat4(model);
-        size_t chunk = max_faces_per_draw > 0 ? size_t(max_faces_per_draw) : size_t(16384);
-        for (uint32_t g = 0; g < mesh->num_groups; ++g) {
-            size_t start = mesh->groups[3 * g], count = mesh->groups[3 * g + 1];
-            std::string name = "m" + std::to_string(mesh->groups[3 * g + 2]);
-            for (size_t s = 0; s < count; s += chunk) {
-                groups.assign(1, AR::MaterialGroup{name, start + s, std::min(chunk, count - s)});
-                pipe->drawMesh(M, m);
-            }
-        }
-        std::memcpy(bgra, fb.getColorData(), size_t(width) * height * 4);
-        std::memcpy(depth, fb.getDepthData(), size_t(width) * height * 4);
-        return 0;
+        return draw_with_camera(cam, mesh, model, shader, width, height, threads, max_faces_per_draw, bgra, depth);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "ref_render: reference threw: %s\n", e.what());
+        return 2;
+    }
+}
+
+// Same draw with an explicit view-projection matrix and eye position installed in the
+// Camera (what drawMesh reads from it, src/tiled_pipeline.cpp:148-155).
+int ref_draw(const axo_mesh* mesh, const float* model, const float* view_proj, const float* cam_pos,
+             const axo_shader* shader, int width, int height, int threads, uint8_t* bgra, float* depth) {
+    const int max_faces_per_draw = 16384;
+    try {
+        AR::Camera cam(glm::vec3(cam_pos[0], cam_pos[1], cam_pos[2]), glm::vec3(0.0f, 0.0f, -1.0f), 60.0f,
+                       float(width) / float(height));
+        cam.setViewport(0, 0, width, height);
+        cam.*member(CamViewProj{}) = load_mat4(view_proj);
+        cam.*member(CamPosition{}) = glm::vec3(cam_pos[0], cam_pos[1], cam_pos[2]);
+        return draw_with_camera(cam, mesh, model, shader, width, height, threads, max_faces_per_draw, bgra, depth);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "ref_draw: reference threw: %s\n", e.what());
         return 2;
     }
 }
