@@ -70,10 +70,10 @@ struct axr_context {
     // device scratch arena
     DevCounters* counters = nullptr;
     LargeTri* large = nullptr;
-    uint32_t* large_next = nullptr;
-    uint32_t large_cap = 0;
+    LargeItem* items = nullptr;
+    uint32_t large_cap = 0, item_cap = 0;
     int collect_stats = 0;
-    int small_max_pixels = 16;
+    int small_max_pixels = 64;
     // profiling: per-draw stage events (4 per draw), reused across reads
     bool profile = false;
     std::vector<cudaEvent_t> event_pool;
@@ -146,23 +146,26 @@ DevTexture dev_texture(const axr_texture* t) {
 }
 
 axr_status grow_scratch(axr_context* ctx, uint32_t faces) {
-    // every face yields at most 8 triangles after clipping; the kernels fall back to
-    // per-thread rasterisation when the list is full, so this bound is a capacity
-    // choice, not a correctness requirement.
-    uint64_t want64 = std::max<uint64_t>(65536, (uint64_t)faces * 2);
-    uint32_t want = (uint32_t)std::min<uint64_t>(want64, 1u << 26);
-    if (want <= ctx->large_cap) return AXR_OK;
+    // Large-triangle setups and tile work items. A triangle that finds either list full is
+    // rasterised by its own thread instead, so these sizes trade memory for speed and are
+    // not needed for correctness.
+    uint32_t want_tris = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(65536, (uint64_t)faces), 1u << 25);
+    uint32_t want_items = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1u << 20, 4ull * faces), 1u << 27);
+    if (want_tris <= ctx->large_cap && want_items <= ctx->item_cap) return AXR_OK;
     if (ctx->capturing)
         return fail(ctx, AXR_E_CAPACITY, "scratch for %u faces not reserved before graph capture", faces);
+    want_tris = std::max(want_tris, ctx->large_cap);
+    want_items = std::max(want_items, ctx->item_cap);
     AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     dfree(ctx->large);
-    dfree(ctx->large_next);
+    dfree(ctx->items);
     ctx->large = nullptr;
-    ctx->large_next = nullptr;
-    ctx->large_cap = 0;
-    AXR_CUDA(ctx, dmalloc(&ctx->large, want));
-    AXR_CUDA(ctx, dmalloc(&ctx->large_next, want));
-    ctx->large_cap = want;
+    ctx->items = nullptr;
+    ctx->large_cap = ctx->item_cap = 0;
+    AXR_CUDA(ctx, dmalloc(&ctx->large, want_tris));
+    AXR_CUDA(ctx, dmalloc(&ctx->items, want_items));
+    ctx->large_cap = want_tris;
+    ctx->item_cap = want_items;
     return AXR_OK;
 }
 
@@ -242,7 +245,7 @@ DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffe
     p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
                          fb->width, fb->height, fb->tiles_x, fb->tiles_y};
     p.u = u;
-    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->large_next, ctx->large_cap, ctx->collect_stats};
+    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->large_cap, ctx->item_cap, ctx->collect_stats, 0};
     p.small_max_pixels = ctx->small_max_pixels;
     return p;
 }
@@ -297,7 +300,7 @@ void axr_context_destroy(axr_context* ctx) {
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     dfree(ctx->counters);
     dfree(ctx->large);
-    dfree(ctx->large_next);
+    dfree(ctx->items);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }

@@ -75,8 +75,8 @@ struct DevUniforms {
     int32_t pad_;
 };
 
-// A triangle too large for the per-thread rasteriser: its setup is stored once and its
-// 16x16 tiles are handed out to warps (64 bytes, one per triangle).
+// A triangle too large for the per-thread rasteriser: its setup is stored once (64 bytes)
+// and each 16x16 tile of its pixel box becomes one work item (LargeItem).
 struct LargeTri {
     float e[9];          // edge a, b, c for edges 0..2 after the area-sign flip
     float inv_area;
@@ -85,17 +85,24 @@ struct LargeTri {
     uint16_t x_lo, x_hi, y_lo, y_hi;  // covered pixel range [lo, hi), clipped to the target
 };
 
+struct LargeItem {
+    uint32_t tri;        // LargeTri index, or kNoItem for a slot reserved but not filled
+    uint32_t tile;       // tile index inside the triangle's tile box (row-major)
+};
+constexpr uint32_t kNoItem = 0xFFFFFFFFu;
+constexpr uint32_t kItemsPerGrab = 4;  // tiles a warp takes per atomic
+
 // Work counters of one draw (all zero between draws; the last CTA of each kernel that
 // consumes a counter resets it).
 struct DevCounters {
-    uint32_t large_count;     // LargeTri entries appended (may exceed capacity: overflow flag)
-    uint32_t large_cursor;    // first entry not yet fully handed out
+    uint32_t large_count;     // LargeTri slots reserved (may exceed the capacity)
+    uint32_t item_count;      // LargeItem slots reserved (may exceed the capacity)
+    uint32_t item_head;       // next LargeItem to hand out
     uint32_t large_done;      // CTAs of the large-triangle kernel that finished
     uint32_t queue_len;       // dirty tiles appended
     uint32_t queue_head;      // dirty tiles handed out
     uint32_t resolve_done;    // CTAs of the resolve kernel that finished
     uint32_t error;           // sticky error bits (kErr*)
-    uint32_t pad_;
     unsigned long long stat_triangles;   // triangles that passed clip + cull
     unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
     unsigned long long stat_large;       // triangles sent to the tile rasteriser
@@ -108,9 +115,11 @@ constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh
 struct DevScratch {
     DevCounters* counters;
     LargeTri* large;
-    uint32_t* large_next;     // per entry: next tile to hand out
+    LargeItem* items;
     uint32_t large_cap;
+    uint32_t item_cap;
     int32_t collect_stats;
+    int32_t pad_;
 };
 
 struct DrawParams {

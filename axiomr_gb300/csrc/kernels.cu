@@ -94,6 +94,13 @@ __device__ __forceinline__ void load_large(const LargeTri* src, Edges& e, uint32
     e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
 }
 
+__device__ __forceinline__ uint32_t tiles_of(const Edges& e, uint32_t& ntx) {
+    int tx0 = e.x_lo >> 4, tx1 = (e.x_hi - 1) >> 4;
+    int ty0 = e.y_lo >> 4, ty1 = (e.y_hi - 1) >> 4;
+    ntx = (uint32_t)(tx1 - tx0 + 1);
+    return ntx * (uint32_t)(ty1 - ty0 + 1);
+}
+
 // Setup of one triangle that survived clipping; rasterises it or queues it as large.
 __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag, GeomStats& st) {
     if (is_backface(s)) return;
@@ -106,20 +113,20 @@ __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag
         st.frags += raster_box(p.target, c, e, tag);
         return;
     }
-    // warp-aggregated append to the large-triangle list
-    unsigned active = __activemask();
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(active) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(&c->large_count, (uint32_t)__popc(active));
-    base = __shfl_sync(active, base, leader);
-    uint32_t slot = base + (uint32_t)__popc(active & ((1u << lane) - 1u));
-    if (slot < p.scratch.large_cap) {
+    // Large triangle: one setup record plus one work item per 16x16 tile of its box.
+    uint32_t ntx;
+    const uint32_t nt = tiles_of(e, ntx);
+    const uint32_t slot = atomicAdd(&c->large_count, 1u);
+    const uint32_t base = atomicAdd(&c->item_count, nt);
+    const uint32_t icap = p.scratch.item_cap;
+    if (slot < p.scratch.large_cap && base + nt <= icap && base + nt > base) {
         store_large(&p.scratch.large[slot], e, tag);
-        p.scratch.large_next[slot] = 0u;
+        for (uint32_t k = 0; k < nt; ++k) p.scratch.items[base + k] = LargeItem{slot, k};
         ++st.large;
     } else {
-        st.frags += raster_box(p.target, c, e, tag);  // list full: rasterise here
+        // lists full: mark any reserved items as empty and rasterise here
+        for (uint32_t k = base; k < icap && k - base < nt; ++k) p.scratch.items[k] = LargeItem{kNoItem, 0u};
+        st.frags += raster_box(p.target, c, e, tag);
     }
 }
 
@@ -174,13 +181,6 @@ __global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant_
     }
 }
 
-__device__ __forceinline__ uint32_t tiles_of(const Edges& e, uint32_t& ntx) {
-    int tx0 = e.x_lo >> 4, tx1 = (e.x_hi - 1) >> 4;
-    int ty0 = e.y_lo >> 4, ty1 = (e.y_hi - 1) >> 4;
-    ntx = (uint32_t)(tx1 - tx0 + 1);
-    return ntx * (uint32_t)(ty1 - ty0 + 1);
-}
-
 // Last CTA out resets the counters this kernel consumed.
 __device__ __forceinline__ bool last_cta(uint32_t* done_counter) {
     __shared__ uint32_t s_last;
@@ -195,48 +195,36 @@ __device__ __forceinline__ bool last_cta(uint32_t* done_counter) {
 
 __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ DrawParams p) {
     DevCounters* c = p.scratch.counters;
-    const uint32_t count = min(*reinterpret_cast<volatile uint32_t*>(&c->large_count), p.scratch.large_cap);
+    const uint32_t n_items = min(*reinterpret_cast<volatile uint32_t*>(&c->item_count), p.scratch.item_cap);
+    const uint32_t n_tris = min(*reinterpret_cast<volatile uint32_t*>(&c->large_count), p.scratch.large_cap);
     const int lane = threadIdx.x & 31;
     uint32_t frags = 0;
     for (;;) {
-        uint32_t entry = 0, item = 0;
-        int have = 0;
-        if (lane == 0) {
-            for (;;) {
-                entry = *reinterpret_cast<volatile uint32_t*>(&c->large_cursor);
-                if (entry >= count) break;
-                const uint32_t* xy = reinterpret_cast<const uint32_t*>(&p.scratch.large[entry]) + 14;
-                Edges e;
-                uint32_t xs = xy[0], ys = xy[1];
-                e.x_lo = (int)(xs & 0xFFFFu); e.x_hi = (int)(xs >> 16);
-                e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
-                uint32_t ntx;
-                uint32_t nt = tiles_of(e, ntx);
-                item = atomicAdd(&p.scratch.large_next[entry], 1u);
-                if (item < nt) { have = 1; break; }
-                atomicCAS(&c->large_cursor, entry, entry + 1u);  // entry exhausted: move on
-            }
-        }
-        have = __shfl_sync(0xFFFFFFFFu, have, 0);
-        if (!have) break;
-        entry = __shfl_sync(0xFFFFFFFFu, entry, 0);
-        item = __shfl_sync(0xFFFFFFFFu, item, 0);
-        Edges e;
-        uint32_t tag;
-        load_large(&p.scratch.large[entry], e, tag);
-        uint32_t ntx;
-        tiles_of(e, ntx);
-        int tx = (e.x_lo >> 4) + (int)(item % ntx);
-        int ty = (e.y_lo >> 4) + (int)(item / ntx);
-        int px = tx * kTile + (lane & 15);
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(&c->item_head, kItemsPerGrab);
+        first = __shfl_sync(0xFFFFFFFFu, first, 0);
+        if (first >= n_items) break;
+        const uint32_t last = min(first + kItemsPerGrab, n_items);
+        for (uint32_t it = first; it < last; ++it) {
+            const LargeItem item = p.scratch.items[it];
+            if (item.tri >= n_tris) continue;  // reserved slot of a triangle rasterised elsewhere
+            Edges e;
+            uint32_t tag;
+            load_large(&p.scratch.large[item.tri], e, tag);
+            uint32_t ntx;
+            tiles_of(e, ntx);
+            const int tx = (e.x_lo >> 4) + (int)(item.tile % ntx);
+            const int ty = (e.y_lo >> 4) + (int)(item.tile / ntx);
+            const int px = tx * kTile + (lane & 15);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            int py = ty * kTile + (lane >> 4) + 2 * r;
-            if (px >= e.x_lo && px < e.x_hi && py >= e.y_lo && py < e.y_hi) {
-                PixelEval pe = eval_pixel(e, px, py);
-                if (pe.covered) {
-                    ++frags;
-                    write_key(p.target, c, px, py, pe.z, tag);
+            for (int r = 0; r < 8; ++r) {
+                const int py = ty * kTile + (lane >> 4) + 2 * r;
+                if (px >= e.x_lo && px < e.x_hi && py >= e.y_lo && py < e.y_hi) {
+                    PixelEval pe = eval_pixel(e, px, py);
+                    if (pe.covered) {
+                        ++frags;
+                        write_key(p.target, c, px, py, pe.z, tag);
+                    }
                 }
             }
         }
@@ -247,7 +235,8 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
     }
     if (last_cta(&c->large_done) && threadIdx.x == 0) {
         c->large_count = 0u;
-        c->large_cursor = 0u;
+        c->item_count = 0u;
+        c->item_head = 0u;
         c->large_done = 0u;
     }
 }
@@ -293,32 +282,23 @@ __device__ void resolve_pixel(const DrawParams& p, int px, int py) {
     t.depth[idx] = r.z;
 }
 
+// One CTA per possible queue slot (the grid covers every tile of the target); CTAs past
+// the number of dirty tiles exit at once, so all dirty tiles are resolved concurrently.
 template <int S>
 __global__ void __launch_bounds__(kBlock) resolve_kernel(const __grid_constant__ DrawParams p) {
-    __shared__ uint32_t s_tile;
     DevCounters* c = p.scratch.counters;
     const DevTarget& t = p.target;
     const uint32_t qlen = *reinterpret_cast<volatile uint32_t*>(&c->queue_len);
-    uint32_t tiles_done = 0;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t q = atomicAdd(&c->queue_head, 1u);
-            s_tile = q < qlen ? t.tile_queue[q] : 0xFFFFFFFFu;
-        }
-        __syncthreads();
-        uint32_t tile = s_tile;
-        __syncthreads();
-        if (tile == 0xFFFFFFFFu) break;
-        int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (threadIdx.x & 15);
-        int py = (int)(tile / (uint32_t)t.tiles_x) * kTile + (threadIdx.x >> 4);
+    if (blockIdx.x < qlen) {
+        const uint32_t tile = t.tile_queue[blockIdx.x];
+        const int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (threadIdx.x & 15);
+        const int py = (int)(tile / (uint32_t)t.tiles_x) * kTile + (threadIdx.x >> 4);
         if (px < t.width && py < t.height) resolve_pixel<S>(p, px, py);
         if (threadIdx.x == 0) {
             t.tile_flag[tile] = 0u;
-            ++tiles_done;
+            if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
         }
     }
-    if (p.scratch.collect_stats && threadIdx.x == 0 && tiles_done)
-        atomicAdd(&c->stat_tiles, (unsigned long long)tiles_done);
     if (last_cta(&c->resolve_done) && threadIdx.x == 0) {
         c->queue_len = 0u;
         c->queue_head = 0u;
@@ -422,8 +402,7 @@ cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     ++*launches;
     if (stage_events && (e = cudaEventRecord(stage_events[2], stream)) != cudaSuccess) return e;
-    unsigned rg = (unsigned)(cfg.num_sms * cfg.resolve_ctas_per_sm);
-    if (rg == 0) rg = 1;
+    unsigned rg = (unsigned)(p.target.tiles_x * p.target.tiles_y);
     switch (p.u.shader) {
         case kFlat: e = launch_resolve<kFlat>(p, rg, stream); break;
         case kPhong: e = launch_resolve<kPhong>(p, rg, stream); break;

@@ -1,0 +1,473 @@
+#!/usr/bin/env python3
+"""Headline benchmark: frames/s of the AxiomR draw path on one GB300.
+
+A step is one frame as the reference renderer produces it (src/renderer.cpp:124-126):
+clearColor + clearDepth + drawMesh of the workload, through the C ABI.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload heightfield|sphere|soup]
+
+`value` is frames/s with every input resident in HBM; L2 is flushed (a 256 MiB write) before
+each timed step and each step is timed with CUDA events on the library's stream. `e2e` is
+the same metric with the mesh arrays and texture uploaded from pinned host memory and the
+framebuffer (colour and depth) read back every step, all inside the timed region.
+`--impl reference` times the CPU restatement of the reference's TiledPipeline (oracle/port,
+all host threads) on the same workload instead. With N > 1 (torchrun), every rank renders
+its own replica of the workload (the path has no cross-GPU exchange); value is the total.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+from axiomr_gb300 import workloads as W  # noqa: E402
+
+WORKLOADS = {
+    "heightfield": (W.heightfield_scene,
+                    "heightfield 1024x1024 vertices (2,093,058 triangles), 2048^2 RGBA8 noise texture, "
+                    "Blinn-Phong, camera 30 deg elevation at distance 2.5, 1920x1080"),
+    "sphere": (W.sphere_scene, "UV sphere 64x32 (3,968 triangles), 256^2 RGBA8 noise texture, Blinn-Phong, "
+                               "camera at distance 3, 512x512"),
+    "soup": (W.soup_scene, "200,000 screen-space triangles (edges 0.5-4 px, depths 0.1-100), Gouraud, 3840x2160"),
+}
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="heightfield")
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            backend = "nccl" if self._cuda() else "gloo"
+            if backend == "nccl":
+                import torch
+
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    @staticmethod
+    def _cuda():
+        try:
+            import torch
+
+            return torch.cuda.is_available()
+        except Exception:
+            return False
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        dev = f"cuda:{self.local_rank}" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def aggregate(step_ms: list, dist: Dist):
+    """Whole-job frames/s: all ranks' frames over the slowest rank's timed total."""
+    total_ms = dist.max(float(sum(step_ms)))
+    frames = len(step_ms) * dist.world
+    return frames / (total_ms / 1e3), total_ms / len(step_ms)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons, power = [], [], set(), []
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, v in zip(self.NAMES, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "power_w_max": max(power) if power else None, "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / f"{kernel}_{workload}.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def pinned_like(lib, arr: np.ndarray, keep: list) -> np.ndarray:
+    """Copy `arr` into page-locked host memory from the library's allocator."""
+    p = lib.axr_host_alloc(arr.nbytes)
+    if not p:
+        raise MemoryError("axr_host_alloc failed")
+    keep.append(p)
+    buf = (C.c_uint8 * arr.nbytes).from_address(p)
+    out = np.frombuffer(buf, dtype=arr.dtype).reshape(arr.shape)
+    out[...] = arr
+    return out
+
+
+def cpu_baseline(scene, steps: int, budget_s: float):
+    """The CPU restatement of the reference pipeline (oracle/port) on all host threads."""
+    from oracle import Oracle
+
+    port = Oracle("port")
+    threads = os.cpu_count() or 1
+    vp = port.camera(scene.camera)[2]
+    t0 = time.perf_counter()
+    port.draw(scene, vp, threads=threads)  # warm-up frame, also sizes the sample
+    t1 = time.perf_counter() - t0
+    frames = max(1, min(steps, int(budget_s / max(t1, 1e-6))))
+    times = []
+    for _ in range(frames):
+        t = time.perf_counter()
+        port.draw(scene, vp, threads=threads)
+        times.append(time.perf_counter() - t)
+    value = len(times) / sum(times)
+    return {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{len(times)} full frames of the workload (clear excluded), median "
+                      f"{statistics.median(times) * 1e3:.1f} ms/frame, host {os.uname().machine}"}
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_ours(args, dist: Dist):
+    import torch
+
+    from axiomr_gb300 import api
+
+    make, desc = WORKLOADS[args.workload]
+    scene = make()
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    ctx = api.Context(dev)
+    lib = ctx.lib
+    fb = api.Framebuffer(ctx, scene.width, scene.height)
+    textures = {}
+    m = scene.mesh
+    shader_kind = scene.shader.kind
+    need_tbn = shader_kind in (W.SHADER_PHONG, W.SHADER_PBR)
+    mats = []
+    images = {}
+
+    def tex(img):
+        if img is None:
+            return None
+        if id(img) not in textures:
+            textures[id(img)] = api.Texture(ctx, img)
+            images[id(img)] = img
+        return textures[id(img)]
+
+    for mat in m.materials:
+        mats.append(api.Material(tex(mat.diffuse), tex(mat.bump), tex(mat.metallic), tex(mat.roughness), tex(mat.ao),
+                                 mat.specular_exponent))
+    mesh = api.Mesh(ctx, m.positions, m.uvs, m.normals, m.indices, m.groups, mats,
+                    m.tangents if need_tbn else None, m.bitangents if need_tbn else None)
+    cam = api.Camera.from_workload(scene.camera)
+    pipe = api.TiledPipeline(ctx, cam, fb)
+    sh = scene.shader
+    pipe.setShader(api.Shader(sh.kind, tuple(sh.light_direction), tuple(sh.light_color)))
+    model = np.asarray(scene.model, np.float32)
+    b, g, r, a = scene.clear_bgra
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def frame():
+        fb.clearColor(r, g, b, a)
+        fb.clearDepth()
+        pipe.drawMesh(model, mesh)
+
+    for _ in range(max(3, args.warmup)):
+        frame()
+    ctx.sync()
+
+    # untimed statistics pass: rasterised fragments and surviving triangles per frame
+    ctx.stats(True)
+    ctx.stats()
+    frame()
+    st = ctx.stats()
+    ctx.stats(False)
+
+    # ---- timed: inputs resident in HBM
+    ctx.profile(True)
+    launches0 = ctx.profile()["kernel_launches"]
+    sampler = ClockSampler(dev)
+    dist.barrier()
+    torch.cuda.synchronize()
+    ctx.sync()
+    sampler.start()
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        frame()
+        e1.record(stream)
+        evs.append((e0, e1))
+    ctx.sync()
+    torch.cuda.synchronize()
+    dist.barrier()
+    sampler.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    prof = ctx.profile()
+    ctx.profile(False)
+    launches = prof["kernel_launches"] - launches0
+    value, ms_per_step = aggregate(step_ms, dist)
+
+    # ---- timed end to end: uploads from pinned host memory and read-back in the region
+    keep = []
+    h_pos = pinned_like(lib, m.positions, keep)
+    h_uv = pinned_like(lib, m.uvs, keep)
+    h_nrm = pinned_like(lib, m.normals, keep)
+    h_idx = pinned_like(lib, m.indices, keep)
+    h_tan = pinned_like(lib, m.tangents, keep) if need_tbn else None
+    h_bit = pinned_like(lib, m.bitangents, keep) if need_tbn else None
+    tex_list = [textures[k] for k in images]
+    h_tex = [pinned_like(lib, np.ascontiguousarray(images[k]), keep) for k in images]
+    h_bgra = pinned_like(lib, np.zeros((scene.height, scene.width, 4), np.uint8), keep)
+    h_depth = pinned_like(lib, np.zeros((scene.height, scene.width), np.float32), keep)
+    h2d = sum(x.nbytes for x in (h_pos, h_uv, h_nrm, h_idx) + tuple(h for h in (h_tan, h_bit) if h is not None))
+    h2d += sum(x.nbytes for x in h_tex)
+    d2h = h_bgra.nbytes + h_depth.nbytes
+
+    def e2e_frame():
+        mesh.update(h_pos, h_uv, h_nrm, h_idx, h_tan, h_bit)
+        for t, img in zip(tex_list, h_tex):
+            t.update(img)
+        frame()
+        C_ok = lib.axr_framebuffer_read_async(ctx.handle, fb.handle, h_bgra.ctypes.data, h_depth.ctypes.data)
+        if C_ok != 0:
+            raise RuntimeError("axr_framebuffer_read_async failed")
+
+    for _ in range(max(3, args.warmup)):
+        e2e_frame()
+    ctx.sync()
+    dist.barrier()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e2e_frame()
+        e1.record(stream)
+        evs.append((e0, e1))
+    ctx.sync()
+    torch.cuda.synchronize()
+    dist.barrier()
+    e2e_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    e2e_value, _ = aggregate(e2e_ms, dist)
+    for p in keep:
+        lib.axr_host_free(p)
+
+    # ---- roofline of the dominant kernel
+    n = max(1, prof["draws"])
+    stage_us = {"geometry": prof["geometry_ms"] / n * 1e3, "large": prof["large_ms"] / n * 1e3,
+                "resolve": prof["resolve_ms"] / n * 1e3}
+    V, F = m.num_vertices, m.num_faces
+    P = scene.width * scene.height
+    frags = st["fragments"]
+    resolved_px = min(P, st["tiles"] * 256)
+    algo_bytes = {
+        # indices + positions read once, one 8-byte depth-key write per covered fragment
+        "geometry": 12.0 * F + 12.0 * V + 8.0 * frags,
+        "large": 8.0 * frags,
+        # per resolved pixel: key read + reset, depth read, colour + depth write; vertex
+        # attributes (position, uv, normal) once
+        "resolve": 28.0 * resolved_px + 32.0 * V,
+    }
+    kernel_names = {"geometry": "geometry_kernel", "large": "large_kernel", "resolve": "resolve_kernel"}
+    dom = max(stage_us, key=stage_us.get)
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = algo_bytes[dom] / (stage_us[dom] * 1e-6) / 1e9
+    traffic = profiled_traffic(kernel_names[dom], args.workload)
+    roofline = {"bound": "hbm", "kernel": kernel_names[dom], "achieved": round(achieved, 1), "peak": hbm_peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                "traffic": traffic, "algorithmic_bytes": algo_bytes[dom], "launch_us": round(stage_us[dom], 2),
+                "stage_us": {k: round(v, 2) for k, v in stage_us.items()}}
+
+    out = {
+        "metric": "frames/s", "value": round(value, 2), "unit": "frames/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
+        "config": {"workload": f"{args.workload}: {desc}", "form": "plain (one drawMesh per frame)",
+                   "l2": "flushed before every timed step (256 MiB write, outside the events)",
+                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},
+        "gfrag_per_s": round(frags * value / 1e9, 3),
+        "mtri_per_s": round(F * value / 1e6, 2),
+        "fragments_per_frame": int(frags), "triangles_per_frame": int(st["triangles"]),
+        "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": sampler.summary(),
+    }
+    ctx.close()
+    return out, scene
+
+
+def run_reference(args, dist: Dist):
+    make, desc = WORKLOADS[args.workload]
+    scene = make()
+    from oracle import Oracle
+
+    port = Oracle("port")
+    threads = os.cpu_count() or 1
+    vp = port.camera(scene.camera)[2]
+    t0 = time.perf_counter()
+    port.draw(scene, vp, threads=threads)
+    t1 = time.perf_counter() - t0
+    for _ in range(max(0, min(args.warmup, int(10.0 / max(t1, 1e-6))) - 1)):
+        port.draw(scene, vp, threads=threads)
+    # each step is one full frame; if K frames would exceed ~3 minutes, a step renders
+    # a contiguous fraction of the faces and counts as that fraction of a frame
+    frac = min(1.0, 180.0 / max(1e-9, args.steps * t1))
+    if frac < 1.0:
+        import dataclasses
+
+        nf = max(1, int(scene.mesh.num_faces * frac))
+        frac = nf / scene.mesh.num_faces
+        scene = dataclasses.replace(scene, mesh=dataclasses.replace(scene.mesh, groups=np.asarray(
+            [[0, nf, 0]], np.uint32)))
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        port.draw(scene, vp, threads=threads)
+        times.append(time.perf_counter() - t)
+    value = frac * len(times) / sum(times)
+    sample = (f"{args.steps} steps, each {'a full frame' if frac >= 1.0 else f'{frac:.3f} of a frame'} "
+              f"of the workload on {threads} host threads ({os.uname().machine})")
+    return {
+        "metric": "frames/s", "value": round(value, 4), "unit": "frames/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
+        "config": {"workload": f"{args.workload}: {desc}", "form": "reference CPU TiledPipeline (C restatement)"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            if dist.rank == 0:
+                print(json.dumps(run_reference(args, dist)), flush=True)
+            return
+        out, scene = run_ours(args, dist)
+        if dist.rank == 0:
+            if dist.world == 1 and not args.no_cpu_baseline:
+                out["cpu_baseline"] = cpu_baseline(scene, args.steps, args.cpu_budget_s)
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()
