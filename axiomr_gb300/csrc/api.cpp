@@ -71,7 +71,10 @@ struct axr_context {
     DevCounters* counters = nullptr;
     LargeTri* large = nullptr;
     LargeItem* items = nullptr;
-    uint32_t large_cap = 0, item_cap = 0;
+    float4* vgeo = nullptr;
+    float4* vattr = nullptr;
+    uint32_t* clip_px = nullptr;
+    uint32_t large_cap = 0, item_cap = 0, vcap = 0, clip_cap = 0;
     int collect_stats = 0;
     int small_max_pixels = 64;
     // profiling: per-draw stage events (4 per draw), reused across reads
@@ -145,27 +148,45 @@ DevTexture dev_texture(const axr_texture* t) {
     return d;
 }
 
-axr_status grow_scratch(axr_context* ctx, uint32_t faces) {
-    // Large-triangle setups and tile work items. A triangle that finds either list full is
-    // rasterised by its own thread instead, so these sizes trade memory for speed and are
-    // not needed for correctness.
+axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uint64_t pixels) {
+    // Large-triangle setups and tile work items (a triangle that finds either list full is
+    // rasterised by its own thread instead, so those two sizes trade memory for speed), the
+    // per-vertex cache of the vertex pass (one entry per vertex) and the clipped-winner
+    // pixel list (at most one entry per pixel).
     uint32_t want_tris = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(65536, (uint64_t)faces), 1u << 25);
     uint32_t want_items = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1u << 20, 4ull * faces), 1u << 27);
-    if (want_tris <= ctx->large_cap && want_items <= ctx->item_cap) return AXR_OK;
+    uint32_t want_verts = std::max<uint32_t>(4096, vertices);
+    uint32_t want_px = (uint32_t)std::max<uint64_t>(1u << 16, pixels);
+    if (want_tris <= ctx->large_cap && want_items <= ctx->item_cap && want_verts <= ctx->vcap &&
+        want_px <= ctx->clip_cap)
+        return AXR_OK;
     if (ctx->capturing)
-        return fail(ctx, AXR_E_CAPACITY, "scratch for %u faces not reserved before graph capture", faces);
+        return fail(ctx, AXR_E_CAPACITY, "scratch for %u faces / %u vertices not reserved before graph capture",
+                    faces, vertices);
     want_tris = std::max(want_tris, ctx->large_cap);
     want_items = std::max(want_items, ctx->item_cap);
+    want_verts = std::max(want_verts, ctx->vcap);
+    want_px = std::max(want_px, ctx->clip_cap);
     AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     dfree(ctx->large);
     dfree(ctx->items);
+    dfree(ctx->vgeo);
+    dfree(ctx->vattr);
+    dfree(ctx->clip_px);
     ctx->large = nullptr;
     ctx->items = nullptr;
-    ctx->large_cap = ctx->item_cap = 0;
+    ctx->vgeo = ctx->vattr = nullptr;
+    ctx->clip_px = nullptr;
+    ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->clip_cap = 0;
     AXR_CUDA(ctx, dmalloc(&ctx->large, want_tris));
     AXR_CUDA(ctx, dmalloc(&ctx->items, want_items));
+    AXR_CUDA(ctx, dmalloc(&ctx->vgeo, 2ull * want_verts));
+    AXR_CUDA(ctx, dmalloc(&ctx->vattr, 4ull * want_verts));
+    AXR_CUDA(ctx, dmalloc(&ctx->clip_px, want_px));
     ctx->large_cap = want_tris;
     ctx->item_cap = want_items;
+    ctx->vcap = want_verts;
+    ctx->clip_cap = want_px;
     return AXR_OK;
 }
 
@@ -245,7 +266,8 @@ DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffe
     p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
                          fb->width, fb->height, fb->tiles_x, fb->tiles_y};
     p.u = u;
-    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->large_cap, ctx->item_cap, ctx->collect_stats, 0};
+    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vgeo, ctx->vattr, ctx->clip_px,
+                           ctx->large_cap, ctx->item_cap, ctx->vcap, ctx->clip_cap, ctx->collect_stats, 0};
     p.small_max_pixels = ctx->small_max_pixels;
     return p;
 }
@@ -301,6 +323,9 @@ void axr_context_destroy(axr_context* ctx) {
     dfree(ctx->counters);
     dfree(ctx->large);
     dfree(ctx->items);
+    dfree(ctx->vgeo);
+    dfree(ctx->vattr);
+    dfree(ctx->clip_px);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -334,7 +359,7 @@ axr_status axr_reserve(axr_context* ctx, uint32_t max_faces) {
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);
     DeviceGuard g(ctx->device);
-    return grow_scratch(ctx, max_faces);
+    return grow_scratch(ctx, max_faces, max_faces * 3u, 3840ull * 2160ull);
 }
 
 void* axr_host_alloc(size_t bytes) {
@@ -630,7 +655,8 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (!ctx->has_shader || !ctx->has_camera || !ctx->fb) return AXR_OK;  // src/tiled_pipeline.cpp:146
     DeviceGuard g(ctx->device);
-    axr_status st = grow_scratch(ctx, mesh->num_drawn);
+    axr_status st = grow_scratch(ctx, mesh->num_drawn, mesh->num_vertices,
+                                 (uint64_t)ctx->fb->width * (uint64_t)ctx->fb->height);
     if (st != AXR_OK) return st;
     DevUniforms u = make_uniforms(ctx->camera, ctx->shader, model);
     DrawParams p = make_params(ctx, mesh, ctx->fb, u);

@@ -92,32 +92,41 @@ struct LargeItem {
 constexpr uint32_t kNoItem = 0xFFFFFFFFu;
 constexpr uint32_t kItemsPerGrab = 4;  // tiles a warp takes per atomic
 
-// Work counters of one draw (all zero between draws; the last CTA of each kernel that
-// consumes a counter resets it).
+// Work counters of one draw: the first kCountersReset bytes are zeroed (a memset on
+// the stream) before every draw.
 struct DevCounters {
     uint32_t large_count;     // LargeTri slots reserved (may exceed the capacity)
     uint32_t item_count;      // LargeItem slots reserved (may exceed the capacity)
     uint32_t item_head;       // next LargeItem to hand out
-    uint32_t large_done;      // CTAs of the large-triangle kernel that finished
     uint32_t queue_len;       // dirty tiles appended
-    uint32_t queue_head;      // dirty tiles handed out
-    uint32_t resolve_done;    // CTAs of the resolve kernel that finished
-    uint32_t error;           // sticky error bits (kErr*)
+    uint32_t clip_count;      // pixels whose winner is a clipped triangle (second resolve pass)
+    uint32_t pad_[2];
+    uint32_t error;           // sticky error bits (kErr*), cleared by axr_sync
     unsigned long long stat_triangles;   // triangles that passed clip + cull
     unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
     unsigned long long stat_large;       // triangles sent to the tile rasteriser
     unsigned long long stat_tiles;       // dirty tiles resolved
 };
 
+constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
 constexpr uint32_t kErrOrdinal = 1u;  // more faces than a depth key can order
 constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh (face skipped)
 
+// Per-vertex cache written by the vertex pass of each draw:
+//   vgeo[2*i]   = (screen x, screen y, NDC z, clip-plane masks as uint bits)
+//   vgeo[2*i+1] = clip-space position (mvp * (x, y, z, 1))
+//   vattr[kMaxVAttr*i ...] = the shader's vertex outputs (VAttr<S> float4s)
 struct DevScratch {
     DevCounters* counters;
     LargeTri* large;
     LargeItem* items;
+    float4* vgeo;
+    float4* vattr;
+    uint32_t* clip_px;        // pixel indices for the clipped-winner resolve pass
     uint32_t large_cap;
     uint32_t item_cap;
+    uint32_t vcap;
+    uint32_t clip_cap;        // >= pixels of the target
     int32_t collect_stats;
     int32_t pad_;
 };

@@ -1,23 +1,31 @@
 // Draw kernels for sm_103a.
 //
-// A draw is three launches on one stream:
-//   geometry_kernel  one thread per face in draw order: vertex transform (mvp * pos),
-//                    homogeneous clipping, backface cull and triangle setup exactly as
-//                    the reference (src/tiled_pipeline.cpp:195-236). Triangles whose
-//                    pixel box is small are rasterised by the same thread; larger ones
-//                    are appended (warp-aggregated atomics) to a list of LargeTri.
-//   large_kernel     persistent warps take (large triangle, 16x16 tile) work items from
-//                    a ragged queue: an entry cursor plus a per-entry tile counter.
-//   resolve_kernel   persistent CTAs take dirty 16x16 tiles from the tile queue, one
-//                    thread per pixel: the pixel's winning triangle is re-derived from
-//                    its depth key, shaded once, and merged into the framebuffer with
-//                    the reference's strict less-than depth test.
-// Visibility is order independent: each covered pixel does a 64-bit atomicMin of
-// (depth, draw-order position), so the surviving key is the reference's early-Z winner
-// (minimum depth, earliest triangle on ties) whatever order the threads run in. Only
-// the winning fragment is shaded; the reference shades every fragment that passes the
-// early test at the time, with the same final colour.
+// A draw is a counter reset (memset) and four launches on one stream:
+//   vertex_kernel    one thread per vertex: clip position (mvp * pos), screen position and
+//                    NDC depth (the per-vertex part of the reference's Triangle ctor,
+//                    src/tiled_pipeline.cpp:53-72), clip-plane masks, and the shader's
+//                    vertex outputs (IShader::vertex, include/shaders/shaders.hpp). The
+//                    reference recomputes these for every face a vertex belongs to (clip
+//                    stage) and every tile a triangle touches (processTile, cpp:407-409);
+//                    they depend only on the vertex, so one evaluation gives the same bits.
+//   geometry_kernel  one thread per face in draw order: clip classification from the
+//                    vertex masks (exact clipper for faces that straddle a plane), backface
+//                    cull and edge setup (cpp:195-236, 436-487). Triangles whose pixel box
+//                    is small are rasterised by the same thread; larger ones get one setup
+//                    record and one work item per 16x16 tile of their box.
+//   large_kernel     warps take tile work items (4 per atomic) and evaluate 256 pixels
+//                    each, 8 per lane.
+//   resolve_kernel   one CTA per dirty 16x16 tile, one thread per pixel: the pixel's winner
+//                    is re-derived from its depth key, shaded once, and merged into the
+//                    framebuffer with the reference's strict less-than test.
+// Visibility is order independent: every covered pixel does a fire-and-forget 64-bit
+// atomicMin of (depth, draw-order position), so the surviving key is the reference's
+// early-Z winner (minimum depth, earliest triangle on ties) whatever order the threads
+// run in. Only the winning fragment is shaded; the reference shades every fragment that
+// passes its early test at the time, with the same final colour.
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include "kernels.h"
 #include "raster.cuh"
@@ -28,48 +36,61 @@ namespace axr {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kTileFlagSet = 1u;
+constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
-__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
-    return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
 
-__device__ __forceinline__ void mark_tile(const DevTarget& t, DevCounters* c, int px, int py) {
-    uint32_t tile = (uint32_t)(py >> 4) * (uint32_t)t.tiles_x + (uint32_t)(px >> 4);
-    if (*reinterpret_cast<volatile uint32_t*>(&t.tile_flag[tile]) == 0u &&
-        atomicExch(&t.tile_flag[tile], kTileFlagSet) == 0u) {
+// First writer of a tile in this draw appends it to the dirty-tile queue (at most one
+// entry per tile per draw, so the queue never exceeds tiles_x * tiles_y).
+__device__ __forceinline__ void mark_tile(const DevTarget& t, DevCounters* c, uint32_t tile) {
+    if (ld_volatile(&t.tile_flag[tile]) == 0u && atomicExch(&t.tile_flag[tile], 1u) == 0u) {
         uint32_t q = atomicAdd(&c->queue_len, 1u);
-        t.tile_queue[q] = tile;  // at most one entry per tile: q < tiles_x * tiles_y
+        t.tile_queue[q] = tile;
     }
 }
 
-// Visibility write of one covered pixel.
-__device__ __forceinline__ void write_key(const DevTarget& t, DevCounters* c, int px, int py, float z, uint32_t tag) {
-    if (!(z < __int_as_float(0x7f800000))) return;  // +inf and NaN never pass early-Z
-    unsigned long long key = make_key(z, tag);
-    unsigned long long* k = &t.key[(size_t)py * (size_t)t.width + (size_t)px];
-    if (key < ld_relaxed(k)) {
-        unsigned long long old = atomicMin(k, key);
-        if (old > key && old == kEmptyKey) mark_tile(t, c, px, py);
-    }
+__device__ __forceinline__ uint32_t tile_of(const DevTarget& t, int px, int py) {
+    return (uint32_t)(py >> 4) * (uint32_t)t.tiles_x + (uint32_t)(px >> 4);
 }
 
-__device__ uint32_t raster_box(const DevTarget& t, DevCounters* c, const Edges& e, uint32_t tag) {
-    uint32_t frags = 0;
-    for (int py = e.y_lo; py < e.y_hi; ++py)
-        for (int px = e.x_lo; px < e.x_hi; ++px) {
-            PixelEval r = eval_pixel(e, px, py);
-            if (r.covered) {
-                ++frags;
-                write_key(t, c, px, py, r.z, tag);
-            }
-        }
-    return frags;
+// Visibility write of one covered pixel (no return value used: compiles to a reduction).
+// Returns whether a key was written.
+__device__ __forceinline__ bool write_key(const DevTarget& t, int px, int py, float z, uint32_t tag) {
+    if (!(z < __int_as_float(0x7f800000))) return false;  // +inf and NaN never pass early-Z
+    atomicMin(&t.key[(size_t)py * (size_t)t.width + (size_t)px], make_key(z, tag));
+    return true;
 }
 
 struct GeomStats {
     uint32_t tris, frags, large;
 };
+
+// Rasterise a small triangle's pixel box in this thread; returns whether any key was written.
+__device__ bool raster_box(const DevTarget& t, const Edges& e, uint32_t tag, GeomStats& st) {
+    bool wrote = false;
+    for (int py = e.y_lo; py < e.y_hi; ++py)
+        for (int px = e.x_lo; px < e.x_hi; ++px) {
+            PixelEval r = eval_pixel(e, px, py);
+            if (r.covered) {
+                ++st.frags;
+                wrote |= write_key(t, px, py, r.z, tag);
+            }
+        }
+    return wrote;
+}
+
+__device__ __forceinline__ uint32_t tiles_of(const Edges& e, uint32_t& ntx) {
+    int tx0 = e.x_lo >> 4, tx1 = (e.x_hi - 1) >> 4;
+    int ty0 = e.y_lo >> 4, ty1 = (e.y_hi - 1) >> 4;
+    ntx = (uint32_t)(tx1 - tx0 + 1);
+    return ntx * (uint32_t)(ty1 - ty0 + 1);
+}
+
+__device__ void mark_box(const DevTarget& t, DevCounters* c, const Edges& e) {
+    for (int ty = e.y_lo >> 4; ty <= (e.y_hi - 1) >> 4; ++ty)
+        for (int tx = e.x_lo >> 4; tx <= (e.x_hi - 1) >> 4; ++tx)
+            mark_tile(t, c, (uint32_t)ty * (uint32_t)t.tiles_x + (uint32_t)tx);
+}
 
 __device__ __forceinline__ void store_large(LargeTri* dst, const Edges& e, uint32_t tag) {
     float4* d = reinterpret_cast<float4*>(dst);
@@ -94,26 +115,27 @@ __device__ __forceinline__ void load_large(const LargeTri* src, Edges& e, uint32
     e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
 }
 
-__device__ __forceinline__ uint32_t tiles_of(const Edges& e, uint32_t& ntx) {
-    int tx0 = e.x_lo >> 4, tx1 = (e.x_hi - 1) >> 4;
-    int ty0 = e.y_lo >> 4, ty1 = (e.y_hi - 1) >> 4;
-    ntx = (uint32_t)(tx1 - tx0 + 1);
-    return ntx * (uint32_t)(ty1 - ty0 + 1);
-}
-
-// Setup of one triangle that survived clipping; rasterises it or queues it as large.
-__device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag, GeomStats& st) {
+// One triangle that survived clipping: cull, set up, then rasterise it here or queue its
+// tiles. *single_tile receives the one tile a small triangle wrote to (the caller marks
+// it after deduplicating across the warp); boxes spanning several tiles are marked here.
+__device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag, GeomStats& st,
+                              uint32_t* single_tile) {
     if (is_backface(s)) return;
     ++st.tris;
     Edges e;
     if (!edge_setup(s, p.target.width, p.target.height, e)) return;
-    int npx = (e.x_hi - e.x_lo) * (e.y_hi - e.y_lo);
+    const int npx = (e.x_hi - e.x_lo) * (e.y_hi - e.y_lo);
     DevCounters* c = p.scratch.counters;
     if (npx <= p.small_max_pixels) {
-        st.frags += raster_box(p.target, c, e, tag);
+        if (raster_box(p.target, e, tag, st)) {
+            uint32_t ntx;
+            if (tiles_of(e, ntx) == 1u && *single_tile == kNoTile)
+                *single_tile = tile_of(p.target, e.x_lo, e.y_lo);
+            else
+                mark_box(p.target, c, e);
+        }
         return;
     }
-    // Large triangle: one setup record plus one work item per 16x16 tile of its box.
     uint32_t ntx;
     const uint32_t nt = tiles_of(e, ntx);
     const uint32_t slot = atomicAdd(&c->large_count, 1u);
@@ -124,79 +146,93 @@ __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag
         for (uint32_t k = 0; k < nt; ++k) p.scratch.items[base + k] = LargeItem{slot, k};
         ++st.large;
     } else {
-        // lists full: mark any reserved items as empty and rasterise here
+        // lists full: mark the reserved items empty and rasterise the triangle here
         for (uint32_t k = base; k < icap && k - base < nt; ++k) p.scratch.items[k] = LargeItem{kNoItem, 0u};
-        st.frags += raster_box(p.target, c, e, tag);
+        if (raster_box(p.target, e, tag, st)) mark_box(p.target, c, e);
     }
+}
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) vertex_kernel(const __grid_constant__ DrawParams p) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= p.mesh.num_vertices) return;
+    constexpr int A = ShaderAttrs<S>::mask;
+    CVFull v = load_vertex<A>(p.mesh, i);
+    f4 clip = mat4_mul(p.u.mvp, v.pos.x, v.pos.y, v.pos.z, 1.0f);
+    f3 sc = screen_vertex(clip, (float)p.target.width, (float)p.target.height);
+    p.scratch.vgeo[2 * (size_t)i] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(plane_masks(clip)));
+    p.scratch.vgeo[2 * (size_t)i + 1] = make_float4(clip.x, clip.y, clip.z, clip.w);
+    pack_vsout<S>(vertex_shader<S>(p.u, v), &p.scratch.vattr[(size_t)kMaxVAttr * i]);
 }
 
 __global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant__ DrawParams p) {
     GeomStats st = {0, 0, 0};
-    uint32_t o = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t single_tile = kNoTile;
+    const uint32_t o = blockIdx.x * kBlock + threadIdx.x;
     if (o < p.mesh.num_drawn) {
         if (o > kMaxOrdinal) {
             atomicOr(&p.scratch.counters->error, kErrOrdinal);
         } else {
-            FaceRef fr = face_of(p.mesh, o);
-            uint3 f = load_face(p.mesh, fr.face);
+            const FaceRef fr = face_of(p.mesh, o);
+            const uint3 f = load_face(p.mesh, fr.face);
             const uint32_t nv = p.mesh.num_vertices;
-            int cls = 0;
-            f4 c0, c1, c2;
             if (f.x >= nv || f.y >= nv || f.z >= nv) {
                 atomicOr(&p.scratch.counters->error, kErrIndex);
             } else {
-                c0 = load_clip(p.mesh, p.u.mvp, f.x);
-                c1 = load_clip(p.mesh, p.u.mvp, f.y);
-                c2 = load_clip(p.mesh, p.u.mvp, f.z);
-                cls = clip_classify(c0, c1, c2);
-            }
-            if (cls == 3) {
-                Screen s;
-                screen_setup(c0, c1, c2, p.target.width, p.target.height, s);
-                emit_triangle(p, s, o << 4, st);
-            } else if (cls < 0) {
-                CVClip a[kMaxClipVerts], b[kMaxClipVerts];
-                a[0].clip = c0; a[1].clip = c1; a[2].clip = c2;
-                CVClip* out;
-                int n = clip_triangle<0>(a, b, &out);
-                for (int j = 0; 3 * j + 2 < n; ++j) {
+                const float4* vg = p.scratch.vgeo;
+                const float4 g0 = __ldg(&vg[2 * (size_t)f.x]), g1 = __ldg(&vg[2 * (size_t)f.y]),
+                             g2 = __ldg(&vg[2 * (size_t)f.z]);
+                const int cls = classify_masks(__float_as_uint(g0.w), __float_as_uint(g1.w), __float_as_uint(g2.w));
+                if (cls == 3) {
                     Screen s;
-                    screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width,
-                                 p.target.height, s);
-                    emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st);
+                    s.x[0] = g0.x; s.y[0] = g0.y; s.z[0] = g0.z;
+                    s.x[1] = g1.x; s.y[1] = g1.y; s.z[1] = g1.z;
+                    s.x[2] = g2.x; s.y[2] = g2.y; s.z[2] = g2.z;
+                    screen_bbox(s);
+                    emit_triangle(p, s, o << 4, st, &single_tile);
+                } else if (cls < 0) {
+                    CVClip a[kMaxClipVerts], b[kMaxClipVerts];
+                    const float4 c0 = __ldg(&vg[2 * (size_t)f.x + 1]), c1 = __ldg(&vg[2 * (size_t)f.y + 1]),
+                                 c2 = __ldg(&vg[2 * (size_t)f.z + 1]);
+                    a[0].clip = mk4(c0.x, c0.y, c0.z, c0.w);
+                    a[1].clip = mk4(c1.x, c1.y, c1.z, c1.w);
+                    a[2].clip = mk4(c2.x, c2.y, c2.z, c2.w);
+                    CVClip* out;
+                    const int n = clip_triangle<0>(a, b, &out);
+                    for (int j = 0; 3 * j + 2 < n; ++j) {
+                        Screen s;
+                        screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width,
+                                     p.target.height, s);
+                        uint32_t tile = kNoTile;
+                        emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile);
+                        if (tile != kNoTile) mark_tile(p.target, p.scratch.counters, tile);
+                    }
                 }
             }
         }
     }
+    // one mark per distinct tile in the warp
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, single_tile);
+    if (single_tile != kNoTile && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1))
+        mark_tile(p.target, p.scratch.counters, single_tile);
     if (p.scratch.collect_stats) {
-        unsigned full = 0xFFFFFFFFu;
-        uint32_t t = __reduce_add_sync(full, st.tris), f = __reduce_add_sync(full, st.frags);
+        const unsigned full = 0xFFFFFFFFu;
+        uint32_t t = __reduce_add_sync(full, st.tris), fr = __reduce_add_sync(full, st.frags);
         uint32_t l = __reduce_add_sync(full, st.large);
         if ((threadIdx.x & 31) == 0) {
             DevCounters* c = p.scratch.counters;
             if (t) atomicAdd(&c->stat_triangles, (unsigned long long)t);
-            if (f) atomicAdd(&c->stat_fragments, (unsigned long long)f);
+            if (fr) atomicAdd(&c->stat_fragments, (unsigned long long)fr);
             if (l) atomicAdd(&c->stat_large, (unsigned long long)l);
         }
     }
 }
 
-// Last CTA out resets the counters this kernel consumed.
-__device__ __forceinline__ bool last_cta(uint32_t* done_counter) {
-    __shared__ uint32_t s_last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = (atomicAdd(done_counter, 1u) == gridDim.x - 1) ? 1u : 0u;
-    }
-    __syncthreads();
-    return s_last != 0u;
-}
-
 __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ DrawParams p) {
     DevCounters* c = p.scratch.counters;
-    const uint32_t n_items = min(*reinterpret_cast<volatile uint32_t*>(&c->item_count), p.scratch.item_cap);
-    const uint32_t n_tris = min(*reinterpret_cast<volatile uint32_t*>(&c->large_count), p.scratch.large_cap);
+    const uint32_t n_items = min(ld_volatile(&c->item_count), p.scratch.item_cap);
+    if (n_items == 0) return;
+    const uint32_t n_tris = min(ld_volatile(&c->large_count), p.scratch.large_cap);
     const int lane = threadIdx.x & 31;
     uint32_t frags = 0;
     for (;;) {
@@ -216,6 +252,7 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
             const int tx = (e.x_lo >> 4) + (int)(item.tile % ntx);
             const int ty = (e.y_lo >> 4) + (int)(item.tile / ntx);
             const int px = tx * kTile + (lane & 15);
+            bool wrote = false;
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
                 const int py = ty * kTile + (lane >> 4) + 2 * r;
@@ -223,63 +260,65 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
                     PixelEval pe = eval_pixel(e, px, py);
                     if (pe.covered) {
                         ++frags;
-                        write_key(p.target, c, px, py, pe.z, tag);
+                        wrote |= write_key(p.target, px, py, pe.z, tag);
                     }
                 }
             }
+            if (__any_sync(0xFFFFFFFFu, wrote) && lane == 0)
+                mark_tile(p.target, c, (uint32_t)ty * (uint32_t)p.target.tiles_x + (uint32_t)tx);
         }
     }
     if (p.scratch.collect_stats) {
         uint32_t f = __reduce_add_sync(0xFFFFFFFFu, frags);
         if (lane == 0 && f) atomicAdd(&c->stat_fragments, (unsigned long long)f);
     }
-    if (last_cta(&c->large_done) && threadIdx.x == 0) {
-        c->large_count = 0u;
-        c->item_count = 0u;
-        c->item_head = 0u;
-        c->large_done = 0u;
-    }
 }
 
-// Re-derive the winning triangle of a pixel from its key tag and shade it.
+// Shade a pixel's winner given its setup and vertex outputs; strict merge into the framebuffer.
 template <int S>
-__device__ void resolve_pixel(const DrawParams& p, int px, int py) {
+__device__ __forceinline__ void shade_winner(const DrawParams& p, size_t idx, int px, int py, uint32_t material,
+                                             Screen& s, const VSOut* vo) {
     const DevTarget& t = p.target;
-    size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
-    unsigned long long key = t.key[idx];
-    if (key == kEmptyKey) return;
-    t.key[idx] = kEmptyKey;
-    const uint32_t tag = (uint32_t)key;
-    constexpr int A = ShaderAttrs<S>::mask;
-    FaceRef fr = face_of(p.mesh, tag >> 4);
-    uint3 f = load_face(p.mesh, fr.face);
-    CVFull v[3];
-    v[0] = load_vertex<A>(p.mesh, f.x);
-    v[1] = load_vertex<A>(p.mesh, f.y);
-    v[2] = load_vertex<A>(p.mesh, f.z);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) v[k].clip = mat4_mul(p.u.mvp, v[k].pos.x, v[k].pos.y, v[k].pos.z, 1.0f);
-    if (tag & 8u) {
-        CVFull a[kMaxClipVerts], b[kMaxClipVerts];
-        a[0] = v[0]; a[1] = v[1]; a[2] = v[2];
-        CVFull* out;
-        int n = clip_triangle<A>(a, b, &out);
-        int j = (int)(tag & 7u);
-        if (3 * j + 2 >= n) return;  // cannot happen: the tag came from this clip
-        v[0] = out[3 * j]; v[1] = out[3 * j + 1]; v[2] = out[3 * j + 2];
-    }
-    Screen s;
-    screen_setup(v[0].clip, v[1].clip, v[2].clip, t.width, t.height, s);
     Edges e;
     if (!edge_setup(s, t.width, t.height, e)) return;
-    PixelEval r = eval_pixel(e, px, py);
+    const PixelEval r = eval_pixel(e, px, py);
     if (!(r.z < t.depth[idx])) return;  // merge: tile depth < framebuffer depth (strict)
-    VSOut vo[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) vo[k] = vertex_shader<S>(p.u, v[k]);
-    f4 col = fragment_shader<S>(p.u, p.mesh.materials[fr.material], mk3(r.alpha, r.beta, r.gamma), vo);
+    const f4 col = fragment_shader<S>(p.u, p.mesh.materials[material], mk3(r.alpha, r.beta, r.gamma), vo);
     t.color[idx] = pack_bgra(col);
     t.depth[idx] = r.z;
+}
+
+// Re-derive the winning triangle of a pixel from its key tag and shade it. Winners that
+// came out of the clipper are deferred to resolve_clipped_kernel (rare, and their path
+// needs the clipper's local arrays and many registers).
+template <int S>
+__device__ __forceinline__ void resolve_pixel(const DrawParams& p, int px, int py) {
+    const DevTarget& t = p.target;
+    const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
+    const unsigned long long key = t.key[idx];
+    if (key == kEmptyKey) return;
+    const uint32_t tag = (uint32_t)key;
+    if (tag & 8u) {
+        const uint32_t slot = atomicAdd(&p.scratch.counters->clip_count, 1u);
+        if (slot < p.scratch.clip_cap) p.scratch.clip_px[slot] = (uint32_t)idx;  // cap >= pixels: always true
+        return;
+    }
+    t.key[idx] = kEmptyKey;
+    const FaceRef fr = face_of(p.mesh, tag >> 4);
+    const uint3 f = load_face(p.mesh, fr.face);
+    Screen s;
+    VSOut vo[3];
+    const uint32_t vi[3] = {f.x, f.y, f.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float4 g = __ldg(&p.scratch.vgeo[2 * (size_t)vi[k]]);
+        s.x[k] = g.x;
+        s.y[k] = g.y;
+        s.z[k] = g.z;
+        vo[k] = unpack_vsout<S>(&p.scratch.vattr[(size_t)kMaxVAttr * vi[k]]);
+    }
+    screen_bbox(s);
+    shade_winner<S>(p, idx, px, py, fr.material, s, vo);
 }
 
 // One CTA per possible queue slot (the grid covers every tile of the target); CTAs past
@@ -288,21 +327,47 @@ template <int S>
 __global__ void __launch_bounds__(kBlock) resolve_kernel(const __grid_constant__ DrawParams p) {
     DevCounters* c = p.scratch.counters;
     const DevTarget& t = p.target;
-    const uint32_t qlen = *reinterpret_cast<volatile uint32_t*>(&c->queue_len);
-    if (blockIdx.x < qlen) {
-        const uint32_t tile = t.tile_queue[blockIdx.x];
-        const int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (threadIdx.x & 15);
-        const int py = (int)(tile / (uint32_t)t.tiles_x) * kTile + (threadIdx.x >> 4);
-        if (px < t.width && py < t.height) resolve_pixel<S>(p, px, py);
-        if (threadIdx.x == 0) {
-            t.tile_flag[tile] = 0u;
-            if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
-        }
+    if (blockIdx.x >= ld_volatile(&c->queue_len)) return;
+    const uint32_t tile = t.tile_queue[blockIdx.x];
+    const int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (threadIdx.x & 15);
+    const int py = (int)(tile / (uint32_t)t.tiles_x) * kTile + (threadIdx.x >> 4);
+    if (px < t.width && py < t.height) resolve_pixel<S>(p, px, py);
+    if (threadIdx.x == 0) {
+        t.tile_flag[tile] = 0u;
+        if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
     }
-    if (last_cta(&c->resolve_done) && threadIdx.x == 0) {
-        c->queue_len = 0u;
-        c->queue_head = 0u;
-        c->resolve_done = 0u;
+}
+
+// Pixels whose winner is a clipped triangle: re-run the clipper on the face's raw vertex
+// attributes (the geometry stage's clip, now carrying attributes; src/pipeline.cpp:243-272)
+// and take output triangle j of the tag.
+template <int S>
+__global__ void __launch_bounds__(kBlock) resolve_clipped_kernel(const __grid_constant__ DrawParams p) {
+    const uint32_t n = min(ld_volatile(&p.scratch.counters->clip_count), p.scratch.clip_cap);
+    constexpr int A = ShaderAttrs<S>::mask;
+    const DevTarget& t = p.target;
+    for (uint32_t q = blockIdx.x * kBlock + threadIdx.x; q < n; q += gridDim.x * kBlock) {
+        const size_t idx = p.scratch.clip_px[q];
+        const uint32_t tag = (uint32_t)t.key[idx];
+        t.key[idx] = kEmptyKey;
+        const int px = (int)(idx % (size_t)t.width), py = (int)(idx / (size_t)t.width);
+        const FaceRef fr = face_of(p.mesh, tag >> 4);
+        const uint3 f = load_face(p.mesh, fr.face);
+        CVFull a[kMaxClipVerts], b[kMaxClipVerts];
+        a[0] = load_vertex<A>(p.mesh, f.x);
+        a[1] = load_vertex<A>(p.mesh, f.y);
+        a[2] = load_vertex<A>(p.mesh, f.z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a[k].clip = mat4_mul(p.u.mvp, a[k].pos.x, a[k].pos.y, a[k].pos.z, 1.0f);
+        CVFull* out;
+        const int cnt = clip_triangle<A>(a, b, &out);
+        const int j = (int)(tag & 7u);
+        if (3 * j + 2 >= cnt) continue;  // cannot happen: the tag came from this clip
+        Screen s;
+        screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, t.width, t.height, s);
+        VSOut vo[3];
+        for (int k = 0; k < 3; ++k) vo[k] = vertex_shader<S>(p.u, out[3 * j + k]);
+        shade_winner<S>(p, idx, px, py, fr.material, s, vo);
     }
 }
 
@@ -336,6 +401,8 @@ __device__ void debug_emit(float* out, uint32_t* count, uint32_t cap, const Scre
     o[10] = s.minx; o[11] = s.miny; o[12] = s.maxx; o[13] = s.maxy;
 }
 
+// Stage dump: the same clip / cull / setup as the geometry kernel, computed from the mesh
+// directly (no vertex cache), writing one record per surviving triangle.
 __global__ void debug_triangles_kernel(const __grid_constant__ DrawParams p, float* out, uint32_t* count,
                                        uint32_t cap) {
     uint32_t o = blockIdx.x * kBlock + threadIdx.x;
@@ -380,41 +447,43 @@ unsigned grid_for(size_t n, int block, unsigned cap = 65535u * 16u) {
 }
 
 template <int S>
-cudaError_t launch_resolve(const DrawParams& p, unsigned grid, cudaStream_t stream) {
-    resolve_kernel<S><<<grid, kBlock, 0, stream>>>(p);
-    return cudaGetLastError();
+cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream, cudaEvent_t* ev,
+                          uint64_t* launches) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(p.scratch.counters, 0, kCountersReset, stream)) != cudaSuccess) return e;
+    if (ev && (e = cudaEventRecord(ev[0], stream)) != cudaSuccess) return e;
+    if (p.mesh.num_drawn > 0) {
+        vertex_kernel<S><<<grid_for(p.mesh.num_vertices, kBlock, 0x7FFFFFFFu), kBlock, 0, stream>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        geometry_kernel<<<grid_for(p.mesh.num_drawn, kBlock, 0x7FFFFFFFu), kBlock, 0, stream>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        *launches += 2;
+    }
+    if (ev && (e = cudaEventRecord(ev[1], stream)) != cudaSuccess) return e;
+    large_kernel<<<(unsigned)(cfg.num_sms * cfg.large_ctas_per_sm), kBlock, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (ev && (e = cudaEventRecord(ev[2], stream)) != cudaSuccess) return e;
+    resolve_kernel<S><<<(unsigned)(p.target.tiles_x * p.target.tiles_y), kBlock, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms, kBlock, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    *launches += 3;
+    if (ev) return cudaEventRecord(ev[3], stream);
+    return cudaSuccess;
 }
 
 }  // namespace
 
 cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream,
                         cudaEvent_t* stage_events, uint64_t* launches) {
-    cudaError_t e;
-    if (stage_events && (e = cudaEventRecord(stage_events[0], stream)) != cudaSuccess) return e;
-    if (p.mesh.num_drawn > 0) {
-        geometry_kernel<<<grid_for(p.mesh.num_drawn, kBlock, 0x7FFFFFFFu), kBlock, 0, stream>>>(p);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
-    }
-    if (stage_events && (e = cudaEventRecord(stage_events[1], stream)) != cudaSuccess) return e;
-    unsigned lg = (unsigned)(cfg.num_sms * cfg.large_ctas_per_sm);
-    large_kernel<<<lg > 0 ? lg : 1, kBlock, 0, stream>>>(p);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    ++*launches;
-    if (stage_events && (e = cudaEventRecord(stage_events[2], stream)) != cudaSuccess) return e;
-    unsigned rg = (unsigned)(p.target.tiles_x * p.target.tiles_y);
     switch (p.u.shader) {
-        case kFlat: e = launch_resolve<kFlat>(p, rg, stream); break;
-        case kPhong: e = launch_resolve<kPhong>(p, rg, stream); break;
-        case kPBR: e = launch_resolve<kPBR>(p, rg, stream); break;
-        case kBlinnPhong: e = launch_resolve<kBlinnPhong>(p, rg, stream); break;
-        case kGouraud: e = launch_resolve<kGouraud>(p, rg, stream); break;
-        default: e = cudaErrorInvalidValue;
+        case kFlat: return launch_shaded<kFlat>(p, cfg, stream, stage_events, launches);
+        case kPhong: return launch_shaded<kPhong>(p, cfg, stream, stage_events, launches);
+        case kPBR: return launch_shaded<kPBR>(p, cfg, stream, stage_events, launches);
+        case kBlinnPhong: return launch_shaded<kBlinnPhong>(p, cfg, stream, stage_events, launches);
+        case kGouraud: return launch_shaded<kGouraud>(p, cfg, stream, stage_events, launches);
+        default: return cudaErrorInvalidValue;
     }
-    if (e != cudaSuccess) return e;
-    ++*launches;
-    if (stage_events) return cudaEventRecord(stage_events[3], stream);
-    return cudaSuccess;
 }
 
 cudaError_t launch_clear(uint32_t* color, float* depth, size_t pixels, uint32_t bgra, float depth_value,

@@ -161,17 +161,16 @@ __device__ __forceinline__ float clamp_w(float w) {
     return w;
 }
 
-__device__ __forceinline__ void screen_setup(f4 c0, f4 c1, f4 c2, int width, int height, Screen& s) {
-    const f4 c[3] = {c0, c1, c2};
-    const float fw = (float)width, fh = (float)height;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        float inv = fdiv(1.0f, clamp_w(c[k].w));
-        s.z[k] = fmul(c[k].z, inv);
-        s.x[k] = fmul(fmul(fadd(fmul(c[k].x, inv), 1.0f), 0.5f), fw);
-        s.y[k] = fmul(fmul(fadd(fmul(c[k].y, inv), 1.0f), 0.5f), fh);
-    }
-    // std::min / std::max over an initializer list: the first of equal values wins
+// Screen position and NDC depth of one clip-space vertex (Triangle ctor, per vertex).
+__device__ __forceinline__ f3 screen_vertex(f4 c, float fw, float fh) {
+    float inv = fdiv(1.0f, clamp_w(c.w));
+    return mk3(fmul(fmul(fadd(fmul(c.x, inv), 1.0f), 0.5f), fw), fmul(fmul(fadd(fmul(c.y, inv), 1.0f), 0.5f), fh),
+               fmul(c.z, inv));
+}
+
+// Bounding box with std::min / std::max over an initializer list: the first of equal
+// values wins and NaN follows operator<.
+__device__ __forceinline__ void screen_bbox(Screen& s) {
     s.minx = s.x[0]; s.miny = s.y[0]; s.maxx = s.x[0]; s.maxy = s.y[0];
 #pragma unroll
     for (int k = 1; k < 3; ++k) {
@@ -180,6 +179,45 @@ __device__ __forceinline__ void screen_setup(f4 c0, f4 c1, f4 c2, int width, int
         if (s.maxx < s.x[k]) s.maxx = s.x[k];
         if (s.maxy < s.y[k]) s.maxy = s.y[k];
     }
+}
+
+__device__ __forceinline__ void screen_setup(f4 c0, f4 c1, f4 c2, int width, int height, Screen& s) {
+    const f4 c[3] = {c0, c1, c2};
+    const float fw = (float)width, fh = (float)height;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f3 v = screen_vertex(c[k], fw, fh);
+        s.x[k] = v.x;
+        s.y[k] = v.y;
+        s.z[k] = v.z;
+    }
+    screen_bbox(s);
+}
+
+// Per-vertex clip-plane classification: bit p set when the vertex is inside plane p
+// (distance >= 0), bit 6+p set when it is outside (distance < 0); a NaN distance sets
+// neither, as the reference's comparisons treat it.
+__device__ __forceinline__ uint32_t plane_masks(f4 c) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        float d = plane_dist(c, p);
+        if (d >= 0.f) m |= 1u << p;
+        if (d < 0.f) m |= 1u << (6 + p);
+    }
+    return m;
+}
+
+// clip_classify from per-vertex masks.
+__device__ __forceinline__ int classify_masks(uint32_t m0, uint32_t m1, uint32_t m2) {
+    const uint32_t all = m0 & m1 & m2;
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        if (all & (1u << p)) continue;
+        if (all & (1u << (6 + p))) return 0;
+        return -1;
+    }
+    return 3;
 }
 
 __device__ __forceinline__ bool is_backface(const Screen& s) {

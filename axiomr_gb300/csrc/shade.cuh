@@ -96,6 +96,60 @@ __device__ __forceinline__ VSOut vertex_shader(const DevUniforms& u, const CVFul
     return o;
 }
 
+// Vertex-shader outputs cached per vertex (float4s per vertex) by the vertex pass:
+//   Flat        [normal, 0]
+//   Gouraud     [normal, uv.x]
+//   BlinnPhong  [world, uv.x] [normal, uv.y]
+//   Phong, PBR  [world, uv.x] [t, uv.y] [b, 0] [n, 0]
+template <int S>
+struct VAttr {
+    static constexpr int n = (S == kPhong || S == kPBR) ? 4 : (S == kBlinnPhong ? 2 : 1);
+};
+constexpr int kMaxVAttr = 4;
+
+template <int S>
+__device__ __forceinline__ void pack_vsout(const VSOut& o, float4* dst) {
+    if constexpr (S == kFlat) {
+        dst[0] = make_float4(o.normal.x, o.normal.y, o.normal.z, 0.0f);
+    } else if constexpr (S == kGouraud) {
+        dst[0] = make_float4(o.normal.x, o.normal.y, o.normal.z, o.uv.x);
+    } else if constexpr (S == kBlinnPhong) {
+        dst[0] = make_float4(o.world.x, o.world.y, o.world.z, o.uv.x);
+        dst[1] = make_float4(o.normal.x, o.normal.y, o.normal.z, o.uv.y);
+    } else {
+        dst[0] = make_float4(o.world.x, o.world.y, o.world.z, o.uv.x);
+        dst[1] = make_float4(o.t.x, o.t.y, o.t.z, o.uv.y);
+        dst[2] = make_float4(o.b.x, o.b.y, o.b.z, 0.0f);
+        dst[3] = make_float4(o.n.x, o.n.y, o.n.z, 0.0f);
+    }
+}
+
+template <int S>
+__device__ __forceinline__ VSOut unpack_vsout(const float4* src) {
+    VSOut o;
+    if constexpr (S == kFlat) {
+        float4 a = __ldg(&src[0]);
+        o.normal = mk3(a.x, a.y, a.z);
+    } else if constexpr (S == kGouraud) {
+        float4 a = __ldg(&src[0]);
+        o.normal = mk3(a.x, a.y, a.z);
+        o.uv = mk2(a.w, 0.0f);
+    } else if constexpr (S == kBlinnPhong) {
+        float4 a = __ldg(&src[0]), b = __ldg(&src[1]);
+        o.world = mk3(a.x, a.y, a.z);
+        o.normal = mk3(b.x, b.y, b.z);
+        o.uv = mk2(a.w, b.w);
+    } else {
+        float4 a = __ldg(&src[0]), b = __ldg(&src[1]), c = __ldg(&src[2]), d = __ldg(&src[3]);
+        o.world = mk3(a.x, a.y, a.z);
+        o.uv = mk2(a.w, b.w);
+        o.t = mk3(b.x, b.y, b.z);
+        o.b = mk3(c.x, c.y, c.z);
+        o.n = mk3(d.x, d.y, d.z);
+    }
+    return o;
+}
+
 // bar.x*a + bar.y*b + bar.z*c, left to right
 __device__ __forceinline__ f3 bary(f3 w, f3 a, f3 b, f3 c) { return add(add(mul(w.x, a), mul(w.y, b)), mul(w.z, c)); }
 __device__ __forceinline__ f2 bary(f3 w, f2 a, f2 b, f2 c) { return add(add(mul(w.x, a), mul(w.y, b)), mul(w.z, c)); }

@@ -1,0 +1,258 @@
+// Header-only C++ facade over the C ABI (axr.h) that keeps the AxiomR class names and
+// call shapes, so renderer code written against the reference reads the same:
+//
+//   reference (namespace AR)                 this facade (namespace axr)
+//   Framebuffer(w, h, true)                  Framebuffer(ctx, w, h)
+//   fb.clearColor(Color) / clearDepth()      same
+//   Texture(path)                            Texture(ctx, rgba, w, h)   (decoding is the caller's)
+//   Mesh(path)                               Mesh(ctx, MeshData)        (OBJ parsing is the caller's)
+//   Camera(pos, target, fov, aspect)         same; update() is implicit
+//   FlatShader / PhongShader / PBRShader     same names, lightDirection / lightColor members
+//   TiledPipeline(threads, cam, fb)          TiledPipeline(ctx, cam, fb)
+//   setShader / setCamera / setFramebuffer   same
+//   drawMesh(modelMatrix, mesh)              same (model is 16 floats, column-major)
+//   Renderer::drawMesh                       Renderer::drawMesh
+//
+// Failures throw axr::Error (the reference throws std exceptions too); the C ABI itself
+// never throws. Every object holds the context it was created on.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "axr.h"
+
+namespace axr {
+
+using Mat4 = std::array<float, 16>;  // column-major
+inline Mat4 identity() { return {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1}; }
+
+struct Error : std::runtime_error {
+    axr_status status;
+    Error(axr_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+};
+
+inline void check(axr_status s, const axr_context* ctx = nullptr) {
+    if (s != AXR_OK) throw Error(s, axr_last_error(ctx));
+}
+
+// Color{r, g, b, a} (reference include/math.hpp:17-19)
+struct Color {
+    unsigned char r, g, b, a;
+};
+
+class Context {
+public:
+    explicit Context(int device = 0) {
+        axr_context* c = nullptr;
+        check(axr_context_create(device, &c));
+        ctx_.reset(c, axr_context_destroy);
+    }
+    axr_context* get() const { return ctx_.get(); }
+    void sync() const { check(axr_sync(ctx_.get()), ctx_.get()); }
+
+private:
+    std::shared_ptr<axr_context> ctx_;
+};
+
+class Texture {
+public:
+    Texture(const Context& ctx, const uint8_t* rgba, int width, int height) : ctx_(ctx) {
+        axr_texture* t = nullptr;
+        check(axr_texture_create(ctx.get(), rgba, width, height, &t), ctx.get());
+        tex_.reset(t, [c = ctx_](axr_texture* p) { axr_texture_destroy(c.get(), p); });
+    }
+    const axr_texture* get() const { return tex_.get(); }
+
+private:
+    Context ctx_;
+    std::shared_ptr<axr_texture> tex_;
+};
+
+// Material (reference include/mesh.hpp:20-34): the textures the shaders read.
+struct Material {
+    std::shared_ptr<Texture> diffuseTexture, bumpTexture, metallicTexture, roughnessTexture, aoTexture;
+    float specularExponent = 1.0f;
+};
+
+// MaterialGroup (reference include/mesh.hpp:35-39) with the material by index.
+struct MaterialGroup {
+    uint32_t startIndex;
+    uint32_t faceCount;
+    uint32_t material;
+};
+
+// Vertex attributes as separate arrays (reference Vertex, include/mesh.hpp:9-18).
+struct MeshData {
+    std::vector<float> positions, uvs, normals, tangents, bitangents;  // 3, 2, 3, 3, 3 per vertex
+    std::vector<uint32_t> indices;                                     // 3 per face
+    std::vector<MaterialGroup> groups;                                 // empty: one group, material 0
+    std::vector<Material> materials;
+};
+
+class Mesh {
+public:
+    Mesh(const Context& ctx, const MeshData& d) : ctx_(ctx), materials_(d.materials) {
+        std::vector<axr_group_desc> groups;
+        for (const MaterialGroup& g : d.groups) groups.push_back({g.startIndex, g.faceCount, g.material});
+        if (groups.empty()) groups.push_back({0u, uint32_t(d.indices.size() / 3), 0u});
+        if (materials_.empty()) materials_.emplace_back();
+        std::vector<axr_material_desc> mats;
+        auto t = [](const std::shared_ptr<Texture>& p) { return p ? p->get() : nullptr; };
+        for (const Material& m : materials_)
+            mats.push_back({t(m.diffuseTexture), t(m.bumpTexture), t(m.metallicTexture), t(m.roughnessTexture),
+                            t(m.aoTexture), m.specularExponent});
+        axr_mesh_desc desc{};
+        desc.num_vertices = uint32_t(d.positions.size() / 3);
+        desc.positions = d.positions.data();
+        desc.uvs = d.uvs.data();
+        desc.normals = d.normals.data();
+        desc.tangents = d.tangents.empty() ? nullptr : d.tangents.data();
+        desc.bitangents = d.bitangents.empty() ? nullptr : d.bitangents.data();
+        desc.num_faces = uint32_t(d.indices.size() / 3);
+        desc.indices = d.indices.data();
+        desc.num_groups = uint32_t(groups.size());
+        desc.groups = groups.data();
+        desc.num_materials = uint32_t(mats.size());
+        desc.materials = mats.data();
+        axr_mesh* m = nullptr;
+        check(axr_mesh_create(ctx.get(), &desc, &m), ctx.get());
+        mesh_.reset(m, [c = ctx_](axr_mesh* p) { axr_mesh_destroy(c.get(), p); });
+    }
+    const axr_mesh* get() const { return mesh_.get(); }
+
+private:
+    Context ctx_;
+    std::vector<Material> materials_;  // keeps the textures alive
+    std::shared_ptr<axr_mesh> mesh_;
+};
+
+class Framebuffer {
+public:
+    Framebuffer(const Context& ctx, int width, int height) : ctx_(ctx), width_(width), height_(height) {
+        axr_framebuffer* f = nullptr;
+        check(axr_framebuffer_create(ctx.get(), width, height, &f), ctx.get());
+        fb_.reset(f, [c = ctx_](axr_framebuffer* p) { axr_framebuffer_destroy(c.get(), p); });
+    }
+    void clearColor(const Color& c) { check(axr_framebuffer_clear_color(ctx_.get(), fb_.get(), c.r, c.g, c.b, c.a), ctx_.get()); }
+    void clearDepth(float v = std::numeric_limits<float>::infinity()) {
+        check(axr_framebuffer_clear_depth(ctx_.get(), fb_.get(), v), ctx_.get());
+    }
+    // BGRA bytes (width*height*4) and depth (width*height) into host memory; blocks.
+    void read(uint8_t* bgra, float* depth) const { check(axr_framebuffer_read(ctx_.get(), fb_.get(), bgra, depth), ctx_.get()); }
+    uint32_t getWidth() const { return uint32_t(width_); }
+    uint32_t getHeight() const { return uint32_t(height_); }
+    axr_framebuffer* get() const { return fb_.get(); }
+
+private:
+    Context ctx_;
+    int width_, height_;
+    std::shared_ptr<axr_framebuffer> fb_;
+};
+
+// Camera (reference include/camera.hpp): matrices of Camera(position, target, fov,
+// aspect) after update(0), near 0.1, far 100.
+class Camera {
+public:
+    Camera(std::array<float, 3> position = {0, 0, 0}, std::array<float, 3> target = {0, 0, -1}, float fov = 60.0f,
+           float aspectRatio = 16.0f / 9.0f)
+        : position_(position) {
+        check(axr_camera_matrices(position.data(), target.data(), fov, aspectRatio, view_.data(), proj_.data(),
+                                  viewProj_.data()));
+        setViewport(0, 0, 800, 600);
+    }
+    void setViewport(int x, int y, int width, int height) { check(axr_viewport_matrix(x, y, width, height, viewport_.data())); }
+    const Mat4& getViewMatrix() const { return view_; }
+    const Mat4& getProjectionMatrix() const { return proj_; }
+    const Mat4& getViewProjectionMatrix() const { return viewProj_; }
+    const Mat4& getViewportMatrix() const { return viewport_; }
+    std::array<float, 3> getPosition() const { return position_; }
+    axr_camera_desc desc() const {
+        axr_camera_desc d{};
+        std::copy(viewProj_.begin(), viewProj_.end(), d.view_proj);
+        std::copy(viewport_.begin(), viewport_.end(), d.viewport);
+        std::copy(position_.begin(), position_.end(), d.position);
+        return d;
+    }
+
+private:
+    std::array<float, 3> position_;
+    Mat4 view_{}, proj_{}, viewProj_{}, viewport_{};
+};
+
+// Shaders (reference include/shaders/shaders.hpp) as descriptors.
+struct IShader {
+    virtual ~IShader() = default;
+    virtual axr_shader_desc desc() const = 0;
+};
+struct FlatShader : IShader {
+    std::array<float, 3> lightDirection{0, -1, 0};
+    axr_shader_desc desc() const override {
+        return {AXR_SHADER_FLAT, {lightDirection[0], lightDirection[1], lightDirection[2]}, {0, 0, 0}};
+    }
+};
+struct LitShader : IShader {
+    std::array<float, 3> lightDirection{0, -1, 0};
+    std::array<float, 3> lightColor{0.6f, 0.6f, 0.6f};
+    virtual int32_t kind() const = 0;
+    axr_shader_desc desc() const override {
+        return {kind(), {lightDirection[0], lightDirection[1], lightDirection[2]},
+                {lightColor[0], lightColor[1], lightColor[2]}};
+    }
+};
+struct PhongShader : LitShader { int32_t kind() const override { return AXR_SHADER_PHONG; } };
+struct PBRShader : LitShader { int32_t kind() const override { return AXR_SHADER_PBR; } };
+struct BlinnPhongShader : LitShader { int32_t kind() const override { return AXR_SHADER_BLINN_PHONG; } };
+struct GouraudShader : IShader {
+    axr_shader_desc desc() const override { return {AXR_SHADER_GOURAUD, {0, 0, 0}, {0, 0, 0}}; }
+};
+
+// TiledPipeline (reference include/tiled_pipeline.hpp:58-62, include/pipeline.hpp:18-48).
+class TiledPipeline {
+public:
+    TiledPipeline(const Context& ctx, Camera* cam = nullptr, Framebuffer* fb = nullptr) : ctx_(ctx) {
+        setCamera(cam);
+        setFramebuffer(fb);
+    }
+    void setShader(const IShader* s) {
+        if (!s) {
+            check(axr_set_shader(ctx_.get(), nullptr), ctx_.get());
+            return;
+        }
+        axr_shader_desc d = s->desc();
+        check(axr_set_shader(ctx_.get(), &d), ctx_.get());
+    }
+    void setCamera(const Camera* c) {
+        if (!c) {
+            check(axr_set_camera(ctx_.get(), nullptr), ctx_.get());
+            return;
+        }
+        axr_camera_desc d = c->desc();
+        check(axr_set_camera(ctx_.get(), &d), ctx_.get());
+    }
+    void setFramebuffer(Framebuffer* fb) { check(axr_set_framebuffer(ctx_.get(), fb ? fb->get() : nullptr), ctx_.get()); }
+    void drawMesh(const Mat4& modelMatrix, const Mesh& mesh) {
+        check(axr_draw_mesh(ctx_.get(), mesh.get(), modelMatrix.data()), ctx_.get());
+    }
+
+private:
+    Context ctx_;
+};
+
+// Renderer::drawMesh (reference src/renderer.cpp:16-19)
+class Renderer {
+public:
+    explicit Renderer(TiledPipeline& p) : pipeline_(p) {}
+    void drawMesh(const Mat4& transMat, const Mesh& mesh) { pipeline_.drawMesh(transMat, mesh); }
+
+private:
+    TiledPipeline& pipeline_;
+};
+
+}  // namespace axr
