@@ -71,10 +71,12 @@ struct axr_context {
     DevCounters* counters = nullptr;
     LargeTri* large = nullptr;
     LargeItem* items = nullptr;
-    float4* vgeo = nullptr;
+    float4* vscreen = nullptr;
+    float4* vclip = nullptr;
     float4* vattr = nullptr;
-    uint32_t* clip_px = nullptr;
-    uint32_t large_cap = 0, item_cap = 0, vcap = 0, clip_cap = 0;
+    uint2* shade = nullptr;
+    uint2* clip_px = nullptr;
+    uint32_t large_cap = 0, item_cap = 0, vcap = 0, px_cap = 0;
     int collect_stats = 0;
     int small_max_pixels = 64;
     // profiling: per-draw stage events (4 per draw), reused across reads
@@ -148,6 +150,21 @@ DevTexture dev_texture(const axr_texture* t) {
     return d;
 }
 
+void free_scratch(axr_context* ctx) {
+    dfree(ctx->large);
+    dfree(ctx->items);
+    dfree(ctx->vscreen);
+    dfree(ctx->vclip);
+    dfree(ctx->vattr);
+    dfree(ctx->shade);
+    dfree(ctx->clip_px);
+    ctx->large = nullptr;
+    ctx->items = nullptr;
+    ctx->vscreen = ctx->vclip = ctx->vattr = nullptr;
+    ctx->shade = ctx->clip_px = nullptr;
+    ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->px_cap = 0;
+}
+
 axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uint64_t pixels) {
     // Large-triangle setups and tile work items (a triangle that finds either list full is
     // rasterised by its own thread instead, so those two sizes trade memory for speed), the
@@ -158,7 +175,7 @@ axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uin
     uint32_t want_verts = std::max<uint32_t>(4096, vertices);
     uint32_t want_px = (uint32_t)std::max<uint64_t>(1u << 16, pixels);
     if (want_tris <= ctx->large_cap && want_items <= ctx->item_cap && want_verts <= ctx->vcap &&
-        want_px <= ctx->clip_cap)
+        want_px <= ctx->px_cap)
         return AXR_OK;
     if (ctx->capturing)
         return fail(ctx, AXR_E_CAPACITY, "scratch for %u faces / %u vertices not reserved before graph capture",
@@ -166,27 +183,20 @@ axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uin
     want_tris = std::max(want_tris, ctx->large_cap);
     want_items = std::max(want_items, ctx->item_cap);
     want_verts = std::max(want_verts, ctx->vcap);
-    want_px = std::max(want_px, ctx->clip_cap);
+    want_px = std::max(want_px, ctx->px_cap);
     AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    dfree(ctx->large);
-    dfree(ctx->items);
-    dfree(ctx->vgeo);
-    dfree(ctx->vattr);
-    dfree(ctx->clip_px);
-    ctx->large = nullptr;
-    ctx->items = nullptr;
-    ctx->vgeo = ctx->vattr = nullptr;
-    ctx->clip_px = nullptr;
-    ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->clip_cap = 0;
+    free_scratch(ctx);
     AXR_CUDA(ctx, dmalloc(&ctx->large, want_tris));
     AXR_CUDA(ctx, dmalloc(&ctx->items, want_items));
-    AXR_CUDA(ctx, dmalloc(&ctx->vgeo, 2ull * want_verts));
+    AXR_CUDA(ctx, dmalloc(&ctx->vscreen, want_verts));
+    AXR_CUDA(ctx, dmalloc(&ctx->vclip, want_verts));
     AXR_CUDA(ctx, dmalloc(&ctx->vattr, 4ull * want_verts));
+    AXR_CUDA(ctx, dmalloc(&ctx->shade, want_px));
     AXR_CUDA(ctx, dmalloc(&ctx->clip_px, want_px));
     ctx->large_cap = want_tris;
     ctx->item_cap = want_items;
     ctx->vcap = want_verts;
-    ctx->clip_cap = want_px;
+    ctx->px_cap = want_px;
     return AXR_OK;
 }
 
@@ -266,8 +276,9 @@ DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffe
     p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
                          fb->width, fb->height, fb->tiles_x, fb->tiles_y};
     p.u = u;
-    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vgeo, ctx->vattr, ctx->clip_px,
-                           ctx->large_cap, ctx->item_cap, ctx->vcap, ctx->clip_cap, ctx->collect_stats, 0};
+    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vscreen, ctx->vclip, ctx->vattr,
+                           ctx->shade, ctx->clip_px, ctx->large_cap, ctx->item_cap, ctx->vcap, ctx->px_cap,
+                           ctx->collect_stats, 0};
     p.small_max_pixels = ctx->small_max_pixels;
     return p;
 }
@@ -321,11 +332,7 @@ void axr_context_destroy(axr_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     dfree(ctx->counters);
-    dfree(ctx->large);
-    dfree(ctx->items);
-    dfree(ctx->vgeo);
-    dfree(ctx->vattr);
-    dfree(ctx->clip_px);
+    free_scratch(ctx);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }

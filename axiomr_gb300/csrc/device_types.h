@@ -100,7 +100,8 @@ struct DevCounters {
     uint32_t item_head;       // next LargeItem to hand out
     uint32_t queue_len;       // dirty tiles appended
     uint32_t clip_count;      // pixels whose winner is a clipped triangle (second resolve pass)
-    uint32_t pad_[2];
+    uint32_t shade_count;     // covered pixels found by the key scan
+    uint32_t pad_;
     uint32_t error;           // sticky error bits (kErr*), cleared by axr_sync
     unsigned long long stat_triangles;   // triangles that passed clip + cull
     unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
@@ -108,25 +109,29 @@ struct DevCounters {
     unsigned long long stat_tiles;       // dirty tiles resolved
 };
 
-constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
+constexpr unsigned kCountersReset = 6 * sizeof(uint32_t);
 constexpr uint32_t kErrOrdinal = 1u;  // more faces than a depth key can order
 constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh (face skipped)
 
 // Per-vertex cache written by the vertex pass of each draw:
-//   vgeo[2*i]   = (screen x, screen y, NDC z, clip-plane masks as uint bits)
-//   vgeo[2*i+1] = clip-space position (mvp * (x, y, z, 1))
-//   vattr[kMaxVAttr*i ...] = the shader's vertex outputs (VAttr<S> float4s)
+//   vscreen[i] = (screen x, screen y, NDC z, clip-plane masks as uint bits)
+//   vclip[i]   = clip-space position (mvp * (x, y, z, 1))
+//   vattr[n*i ...] = the shader's vertex outputs (n = VAttr<S>::n float4s)
+// Resolve work lists: shade[k] = (pixel index, depth-key tag) of every covered pixel of
+// the dirty tiles; clip_px[k] = the same pair for every pixel whose winner was clipped.
 struct DevScratch {
     DevCounters* counters;
     LargeTri* large;
     LargeItem* items;
-    float4* vgeo;
+    float4* vscreen;
+    float4* vclip;
     float4* vattr;
-    uint32_t* clip_px;        // pixel indices for the clipped-winner resolve pass
+    uint2* shade;
+    uint2* clip_px;
     uint32_t large_cap;
     uint32_t item_cap;
     uint32_t vcap;
-    uint32_t clip_cap;        // >= pixels of the target
+    uint32_t px_cap;          // >= pixels of the target (shade and clip_px capacity)
     int32_t collect_stats;
     int32_t pad_;
 };

@@ -1,6 +1,6 @@
 // Draw kernels for sm_103a.
 //
-// A draw is a counter reset (memset) and four launches on one stream:
+// A draw is a counter reset (memset) and six launches on one stream:
 //   vertex_kernel    one thread per vertex: clip position (mvp * pos), screen position and
 //                    NDC depth (the per-vertex part of the reference's Triangle ctor,
 //                    src/tiled_pipeline.cpp:53-72), clip-plane masks, and the shader's
@@ -15,9 +15,12 @@
 //                    record and one work item per 16x16 tile of their box.
 //   large_kernel     warps take tile work items (4 per atomic) and evaluate 256 pixels
 //                    each, 8 per lane.
-//   resolve_kernel   one CTA per dirty 16x16 tile, one thread per pixel: the pixel's winner
-//                    is re-derived from its depth key, shaded once, and merged into the
-//                    framebuffer with the reference's strict less-than test.
+//   scan_kernel      one warp per dirty 16x16 tile: compacts the tile's covered pixels
+//                    (non-empty depth keys) into a shade list and resets the keys.
+//   shade_kernel     one thread per covered pixel: the winner is re-derived from its depth
+//                    key, shaded once, and merged into the framebuffer with the reference's
+//                    strict less-than test (winners that were clipped go to
+//                    resolve_clipped_kernel).
 // Visibility is order independent: every covered pixel does a fire-and-forget 64-bit
 // atomicMin of (depth, draw-order position), so the surviving key is the reference's
 // early-Z winner (minimum depth, earliest triangle on ties) whatever order the threads
@@ -65,17 +68,43 @@ struct GeomStats {
     uint32_t tris, frags, large;
 };
 
-// Rasterise a small triangle's pixel box in this thread; returns whether any key was written.
+// Rasterise a small triangle's pixel box in this thread; returns whether any key was
+// written. Walks the box the way the reference's tile raster does: per 16-pixel tile
+// column and row, the row start (a*(sx+0.5) + b*(py+0.5)) + c and its 8-pixel step are
+// computed once, then each pixel adds a*lane (eval_pixel gives the same bits per pixel).
 __device__ bool raster_box(const DevTarget& t, const Edges& e, uint32_t tag, GeomStats& st) {
     bool wrote = false;
-    for (int py = e.y_lo; py < e.y_hi; ++py)
-        for (int px = e.x_lo; px < e.x_hi; ++px) {
-            PixelEval r = eval_pixel(e, px, py);
-            if (r.covered) {
-                ++st.frags;
-                wrote |= write_key(t, px, py, r.z, tag);
+    for (int tx = e.x_lo >> 4; tx <= (e.x_hi - 1) >> 4; ++tx) {
+        const int sx = max(tx * kTile, e.x_lo);
+        const int ex = min((tx + 1) * kTile, e.x_hi);
+        const float fsx = fadd((float)sx, 0.5f);
+        float as[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) as[k] = fmul(e.a[k], fsx);
+        for (int py = e.y_lo; py < e.y_hi; ++py) {
+            const float fpy = fadd((float)py, 0.5f);
+            float r0[3], r8[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                r0[k] = fadd(fadd(as[k], fmul(e.b[k], fpy)), e.c[k]);
+                r8[k] = fadd(r0[k], fmul(e.a[k], 8.0f));
+            }
+            for (int px = sx; px < ex; ++px) {
+                const int i = px - sx;
+                const float lane = (float)(i & 7);
+                float cov[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) cov[k] = fadd(i >= 8 ? r8[k] : r0[k], fmul(e.a[k], lane));
+                if (cov[0] >= 0.f && cov[1] >= 0.f && cov[2] >= 0.f) {
+                    ++st.frags;
+                    const float al = fmul(cov[0], e.inv_area), be = fmul(cov[1], e.inv_area),
+                                ga = fmul(cov[2], e.inv_area);
+                    const float z = fadd(fadd(fmul(e.z[0], al), fmul(e.z[1], be)), fmul(e.z[2], ga));
+                    wrote |= write_key(t, px, py, z, tag);
+                }
             }
         }
+    }
     return wrote;
 }
 
@@ -160,9 +189,9 @@ __global__ void __launch_bounds__(kBlock) vertex_kernel(const __grid_constant__ 
     CVFull v = load_vertex<A>(p.mesh, i);
     f4 clip = mat4_mul(p.u.mvp, v.pos.x, v.pos.y, v.pos.z, 1.0f);
     f3 sc = screen_vertex(clip, (float)p.target.width, (float)p.target.height);
-    p.scratch.vgeo[2 * (size_t)i] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(plane_masks(clip)));
-    p.scratch.vgeo[2 * (size_t)i + 1] = make_float4(clip.x, clip.y, clip.z, clip.w);
-    pack_vsout<S>(vertex_shader<S>(p.u, v), &p.scratch.vattr[(size_t)kMaxVAttr * i]);
+    p.scratch.vscreen[i] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(plane_masks(clip)));
+    p.scratch.vclip[i] = make_float4(clip.x, clip.y, clip.z, clip.w);
+    pack_vsout<S>(vertex_shader<S>(p.u, v), &p.scratch.vattr[(size_t)VAttr<S>::n * i]);
 }
 
 __global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant__ DrawParams p) {
@@ -179,9 +208,8 @@ __global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant_
             if (f.x >= nv || f.y >= nv || f.z >= nv) {
                 atomicOr(&p.scratch.counters->error, kErrIndex);
             } else {
-                const float4* vg = p.scratch.vgeo;
-                const float4 g0 = __ldg(&vg[2 * (size_t)f.x]), g1 = __ldg(&vg[2 * (size_t)f.y]),
-                             g2 = __ldg(&vg[2 * (size_t)f.z]);
+                const float4* vs = p.scratch.vscreen;
+                const float4 g0 = __ldg(&vs[f.x]), g1 = __ldg(&vs[f.y]), g2 = __ldg(&vs[f.z]);
                 const int cls = classify_masks(__float_as_uint(g0.w), __float_as_uint(g1.w), __float_as_uint(g2.w));
                 if (cls == 3) {
                     Screen s;
@@ -192,8 +220,8 @@ __global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant_
                     emit_triangle(p, s, o << 4, st, &single_tile);
                 } else if (cls < 0) {
                     CVClip a[kMaxClipVerts], b[kMaxClipVerts];
-                    const float4 c0 = __ldg(&vg[2 * (size_t)f.x + 1]), c1 = __ldg(&vg[2 * (size_t)f.y + 1]),
-                                 c2 = __ldg(&vg[2 * (size_t)f.z + 1]);
+                    const float4* vc = p.scratch.vclip;
+                    const float4 c0 = __ldg(&vc[f.x]), c1 = __ldg(&vc[f.y]), c2 = __ldg(&vc[f.z]);
                     a[0].clip = mk4(c0.x, c0.y, c0.z, c0.w);
                     a[1].clip = mk4(c1.x, c1.y, c1.z, c1.w);
                     a[2].clip = mk4(c2.x, c2.y, c2.z, c2.w);
@@ -274,6 +302,46 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
     }
 }
 
+// Key scan: one warp per dirty tile (grid-stride over the tile queue) reads the tile's 256
+// keys, 8 per lane, appends (pixel, tag) of every covered pixel to the shade list
+// (warp-aggregated), resets those keys and clears the tile flag.
+__global__ void __launch_bounds__(kBlock) scan_kernel(const __grid_constant__ DrawParams p) {
+    DevCounters* c = p.scratch.counters;
+    const DevTarget& t = p.target;
+    const uint32_t qlen = ld_volatile(&c->queue_len);
+    const int lane = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * (kBlock / 32);
+    for (uint32_t q = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); q < qlen; q += nwarps) {
+        const uint32_t tile = t.tile_queue[q];
+        const int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (lane & 15);
+        const int py0 = (int)(tile / (uint32_t)t.tiles_x) * kTile + (lane >> 4);
+        unsigned long long keys[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int py = py0 + 2 * r;
+            keys[r] = (px < t.width && py < t.height) ? t.key[(size_t)py * (size_t)t.width + (size_t)px] : kEmptyKey;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const bool has = keys[r] != kEmptyKey;
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, has);
+            if (m == 0u) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&c->shade_count, (uint32_t)__popc(m));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (has) {
+                const uint32_t idx = (uint32_t)((size_t)(py0 + 2 * r) * (size_t)t.width + (size_t)px);
+                p.scratch.shade[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = make_uint2(idx, (uint32_t)keys[r]);
+                t.key[idx] = kEmptyKey;
+            }
+        }
+        if (lane == 0) {
+            t.tile_flag[tile] = 0u;
+            if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
+        }
+    }
+}
+
 // Shade a pixel's winner given its setup and vertex outputs; strict merge into the framebuffer.
 template <int S>
 __device__ __forceinline__ void shade_winner(const DrawParams& p, size_t idx, int px, int py, uint32_t material,
@@ -288,53 +356,40 @@ __device__ __forceinline__ void shade_winner(const DrawParams& p, size_t idx, in
     t.depth[idx] = r.z;
 }
 
-// Re-derive the winning triangle of a pixel from its key tag and shade it. Winners that
-// came out of the clipper are deferred to resolve_clipped_kernel (rare, and their path
-// needs the clipper's local arrays and many registers).
+// Dense shading of the covered pixels: the winner is re-derived from its tag (face ->
+// cached vertex screen positions and shader outputs), its barycentrics recomputed exactly
+// and the fragment shaded once. Winners that came out of the clipper go to the clipped
+// list (resolve_clipped_kernel).
 template <int S>
-__device__ __forceinline__ void resolve_pixel(const DrawParams& p, int px, int py) {
-    const DevTarget& t = p.target;
-    const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
-    const unsigned long long key = t.key[idx];
-    if (key == kEmptyKey) return;
-    const uint32_t tag = (uint32_t)key;
-    if (tag & 8u) {
-        const uint32_t slot = atomicAdd(&p.scratch.counters->clip_count, 1u);
-        if (slot < p.scratch.clip_cap) p.scratch.clip_px[slot] = (uint32_t)idx;  // cap >= pixels: always true
-        return;
-    }
-    t.key[idx] = kEmptyKey;
-    const FaceRef fr = face_of(p.mesh, tag >> 4);
-    const uint3 f = load_face(p.mesh, fr.face);
-    Screen s;
-    VSOut vo[3];
-    const uint32_t vi[3] = {f.x, f.y, f.z};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float4 g = __ldg(&p.scratch.vgeo[2 * (size_t)vi[k]]);
-        s.x[k] = g.x;
-        s.y[k] = g.y;
-        s.z[k] = g.z;
-        vo[k] = unpack_vsout<S>(&p.scratch.vattr[(size_t)kMaxVAttr * vi[k]]);
-    }
-    screen_bbox(s);
-    shade_winner<S>(p, idx, px, py, fr.material, s, vo);
-}
-
-// One CTA per possible queue slot (the grid covers every tile of the target); CTAs past
-// the number of dirty tiles exit at once, so all dirty tiles are resolved concurrently.
-template <int S>
-__global__ void __launch_bounds__(kBlock) resolve_kernel(const __grid_constant__ DrawParams p) {
+__global__ void __launch_bounds__(kBlock) shade_kernel(const __grid_constant__ DrawParams p) {
     DevCounters* c = p.scratch.counters;
     const DevTarget& t = p.target;
-    if (blockIdx.x >= ld_volatile(&c->queue_len)) return;
-    const uint32_t tile = t.tile_queue[blockIdx.x];
-    const int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (threadIdx.x & 15);
-    const int py = (int)(tile / (uint32_t)t.tiles_x) * kTile + (threadIdx.x >> 4);
-    if (px < t.width && py < t.height) resolve_pixel<S>(p, px, py);
-    if (threadIdx.x == 0) {
-        t.tile_flag[tile] = 0u;
-        if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
+    const uint32_t n = min(ld_volatile(&c->shade_count), p.scratch.px_cap);
+    for (uint32_t q = blockIdx.x * kBlock + threadIdx.x; q < n; q += gridDim.x * kBlock) {
+        const uint2 w = p.scratch.shade[q];
+        const uint32_t tag = w.y;
+        if (tag & 8u) {
+            const uint32_t slot = atomicAdd(&c->clip_count, 1u);
+            p.scratch.clip_px[slot] = w;  // at most one entry per pixel: slot < px_cap
+            continue;
+        }
+        const size_t idx = w.x;
+        const int px = (int)(idx % (size_t)t.width), py = (int)(idx / (size_t)t.width);
+        const FaceRef fr = face_of(p.mesh, tag >> 4);
+        const uint3 f = load_face(p.mesh, fr.face);
+        Screen s;
+        VSOut vo[3];
+        const uint32_t vi[3] = {f.x, f.y, f.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float4 g = __ldg(&p.scratch.vscreen[vi[k]]);
+            s.x[k] = g.x;
+            s.y[k] = g.y;
+            s.z[k] = g.z;
+            vo[k] = unpack_vsout<S>(&p.scratch.vattr[(size_t)VAttr<S>::n * vi[k]]);
+        }
+        screen_bbox(s);
+        shade_winner<S>(p, idx, px, py, fr.material, s, vo);
     }
 }
 
@@ -343,13 +398,13 @@ __global__ void __launch_bounds__(kBlock) resolve_kernel(const __grid_constant__
 // and take output triangle j of the tag.
 template <int S>
 __global__ void __launch_bounds__(kBlock) resolve_clipped_kernel(const __grid_constant__ DrawParams p) {
-    const uint32_t n = min(ld_volatile(&p.scratch.counters->clip_count), p.scratch.clip_cap);
+    const uint32_t n = min(ld_volatile(&p.scratch.counters->clip_count), p.scratch.px_cap);
     constexpr int A = ShaderAttrs<S>::mask;
     const DevTarget& t = p.target;
     for (uint32_t q = blockIdx.x * kBlock + threadIdx.x; q < n; q += gridDim.x * kBlock) {
-        const size_t idx = p.scratch.clip_px[q];
-        const uint32_t tag = (uint32_t)t.key[idx];
-        t.key[idx] = kEmptyKey;
+        const uint2 w = p.scratch.clip_px[q];
+        const size_t idx = w.x;
+        const uint32_t tag = w.y;
         const int px = (int)(idx % (size_t)t.width), py = (int)(idx / (size_t)t.width);
         const FaceRef fr = face_of(p.mesh, tag >> 4);
         const uint3 f = load_face(p.mesh, fr.face);
@@ -371,10 +426,18 @@ __global__ void __launch_bounds__(kBlock) resolve_clipped_kernel(const __grid_co
     }
 }
 
+// Colour and/or depth fill, 16-byte stores (the planes are 256-byte aligned allocations).
 __global__ void clear_kernel(uint32_t* color, float* depth, size_t n, uint32_t bgra, float dv, int do_color,
                              int do_depth) {
-    size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t n4 = n / 4;
+    const uint4 cv = make_uint4(bgra, bgra, bgra, bgra);
+    const float4 dv4 = make_float4(dv, dv, dv, dv);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        if (do_color) reinterpret_cast<uint4*>(color)[i] = cv;
+        if (do_depth) reinterpret_cast<float4*>(depth)[i] = dv4;
+    }
+    for (size_t i = 4 * n4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         if (do_color) color[i] = bgra;
         if (do_depth) depth[i] = dv;
     }
@@ -463,11 +526,14 @@ cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStre
     large_kernel<<<(unsigned)(cfg.num_sms * cfg.large_ctas_per_sm), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (ev && (e = cudaEventRecord(ev[2], stream)) != cudaSuccess) return e;
-    resolve_kernel<S><<<(unsigned)(p.target.tiles_x * p.target.tiles_y), kBlock, 0, stream>>>(p);
+    const unsigned tiles = (unsigned)(p.target.tiles_x * p.target.tiles_y);
+    scan_kernel<<<min((tiles + 7u) / 8u, (unsigned)(cfg.num_sms * 8)), kBlock, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    shade_kernel<S><<<(unsigned)(cfg.num_sms * cfg.resolve_ctas_per_sm), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms, kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    *launches += 3;
+    *launches += 4;
     if (ev) return cudaEventRecord(ev[3], stream);
     return cudaSuccess;
 }
