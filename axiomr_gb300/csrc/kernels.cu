@@ -321,18 +321,27 @@ __global__ void __launch_bounds__(kBlock) scan_kernel(const __grid_constant__ Dr
             const int py = py0 + 2 * r;
             keys[r] = (px < t.width && py < t.height) ? t.key[(size_t)py * (size_t)t.width + (size_t)px] : kEmptyKey;
         }
+        // one atomic per tile: per-row ballots give each covered pixel its slot
+        unsigned m[8];
+        uint32_t total = 0;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            const bool has = keys[r] != kEmptyKey;
-            const unsigned m = __ballot_sync(0xFFFFFFFFu, has);
-            if (m == 0u) continue;
+            m[r] = __ballot_sync(0xFFFFFFFFu, keys[r] != kEmptyKey);
+            total += (uint32_t)__popc(m[r]);
+        }
+        if (total != 0u) {
             uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(&c->shade_count, (uint32_t)__popc(m));
+            if (lane == 0) base = atomicAdd(&c->shade_count, total);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (has) {
-                const uint32_t idx = (uint32_t)((size_t)(py0 + 2 * r) * (size_t)t.width + (size_t)px);
-                p.scratch.shade[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = make_uint2(idx, (uint32_t)keys[r]);
-                t.key[idx] = kEmptyKey;
+            const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                if (keys[r] != kEmptyKey) {
+                    const uint32_t idx = (uint32_t)((size_t)(py0 + 2 * r) * (size_t)t.width + (size_t)px);
+                    p.scratch.shade[base + (uint32_t)__popc(m[r] & below)] = make_uint2(idx, (uint32_t)keys[r]);
+                    t.key[idx] = kEmptyKey;
+                }
+                base += (uint32_t)__popc(m[r]);
             }
         }
         if (lane == 0) {
