@@ -96,6 +96,7 @@ SIGNATURES = {
     "axr_set_camera": (S, [P, P]),
     "axr_set_framebuffer": (S, [P, P]),
     "axr_draw_mesh": (S, [P, P, P]),
+    "axr_draw_mesh_noalloc": (S, [P, P, P]),
     "axr_draw_batch": (S, [P, P, C.c_int32]),
     "axr_graph_begin": (S, [P]),
     "axr_graph_end": (S, [P, PP]),

@@ -1,0 +1,109 @@
+// Definitions behind the C ABI's opaque handles (include/axr.h), shared by the .cu/.cpp
+// files that implement entry points, plus the per-draw uniform computation.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "axr.h"
+#include "device_types.h"
+#include "hostmath.h"
+#include "kernels.h"
+
+using axr::DevCounters;
+using axr::DevGroup;
+using axr::DevMaterial;
+using axr::LargeItem;
+using axr::LargeTri;
+using axr::LaunchConfig;
+
+struct axr_texture {
+    uint32_t* texels = nullptr;
+    int32_t width = 0, height = 0;
+    int device = 0;
+};
+
+struct axr_mesh {
+    float4* pos = nullptr;
+    float4* nrm = nullptr;
+    float4* tan = nullptr;
+    float4* bit = nullptr;
+    float2* uv = nullptr;
+    uint32_t* idx = nullptr;
+    DevGroup* groups = nullptr;
+    DevMaterial* materials = nullptr;
+    float* staging = nullptr;  // packed float3 upload area for updates
+    uint32_t num_vertices = 0, num_faces = 0, num_groups = 0, num_materials = 0, num_drawn = 0;
+    int device = 0;
+};
+
+struct axr_framebuffer {
+    uint32_t* color = nullptr;
+    float* depth = nullptr;
+    unsigned long long* key = nullptr;
+    uint32_t* tile_flag = nullptr;
+    uint32_t* tile_queue = nullptr;
+    int32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
+    int device = 0;
+};
+
+struct axr_graph {
+    cudaGraphExec_t exec = nullptr;
+    int device = 0;
+};
+
+struct axr_context {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    LaunchConfig cfg{};
+    std::mutex mu;
+    std::string error;
+    bool capturing = false;
+    // pipeline state (Pipeline::m_Shader, m_Camera, m_Framebuffer)
+    bool has_shader = false, has_camera = false;
+    axr_shader_desc shader{};
+    axr_camera_desc camera{};
+    axr_framebuffer* fb = nullptr;
+    // device scratch arena
+    DevCounters* counters = nullptr;
+    LargeTri* large = nullptr;
+    LargeItem* items = nullptr;
+    float4* vscreen = nullptr;
+    float4* vclip = nullptr;
+    float4* vattr = nullptr;
+    uint2* shade = nullptr;
+    uint2* clip_px = nullptr;
+    uint32_t large_cap = 0, item_cap = 0, vcap = 0, px_cap = 0;
+    int collect_stats = 0;
+    int small_max_pixels = 64;
+    // profiling: per-draw stage events (4 per draw), reused across reads
+    bool profile = false;
+    std::vector<cudaEvent_t> event_pool;
+    size_t events_used = 0;
+    uint64_t launches = 0;
+};
+
+namespace axr {
+
+// Uniforms the draw kernels read: mvp = viewProj * modelMatrix (src/tiled_pipeline.cpp:149)
+// in the kernels' association order, the Flat shader's normal matrix, eye and lights.
+inline DevUniforms make_uniforms(const axr_camera_desc& cam, const axr_shader_desc& sh, const float* model) {
+    DevUniforms u{};
+    host::M4 vp = host::load(cam.view_proj);
+    host::M4 mm = host::load(model);
+    host::M4 mvp = host::mul(vp, mm);  // viewProj * modelMatrix (src/tiled_pipeline.cpp:149)
+    std::memcpy(u.mvp, mvp.m, sizeof(u.mvp));
+    std::memcpy(u.model, model, sizeof(u.model));
+    if (sh.kind == AXR_SHADER_FLAT) host::normal_matrix(mm, u.normal_mat);
+    std::memcpy(u.cam_pos, cam.position, sizeof(u.cam_pos));
+    std::memcpy(u.light_dir, sh.light_direction, sizeof(u.light_dir));
+    std::memcpy(u.light_color, sh.light_color, sizeof(u.light_color));
+    u.shader = sh.kind;
+    return u;
+}
+
+}  // namespace axr

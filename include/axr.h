@@ -187,6 +187,17 @@ axr_status axr_set_framebuffer(axr_context* ctx, axr_framebuffer* fb);
  * framebuffer set does nothing (src/tiled_pipeline.cpp:146). */
 axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
 
+/* No counterpart in the reference. The same draw as axr_draw_mesh for callers that cannot
+ * allocate device memory: a renderer recording its frame into a CUDA graph, a real-time
+ * loop that forbids allocator calls after start-up, or a host that owns the device-memory
+ * budget. Its scratch lives in one fixed device array inside the library (about 28 MiB,
+ * reserved on every GPU that loads the library until exit), so the call allocates nothing.
+ * Limits: 65536 vertices, 65536 drawn faces, 1024*1024 framebuffer pixels; larger draws
+ * return AXR_E_CAPACITY. The first call on a device looks up the array's address, so make
+ * it before any stream capture. All calls share the array: calls whose work overlaps on
+ * the GPU (other streams or contexts) race. */
+axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
+
 /* ------------------------------------------------------------------ batched form
  * Many independent draws (each with its own framebuffer, camera, shader and mesh) in
  * one persistent launch over a shared work queue; no reference counterpart (the
