@@ -52,8 +52,9 @@ class DrawDesc(C.Structure):
 
 
 class Profile(C.Structure):
-    _fields_ = [("draws", C.c_uint32), ("pad_", C.c_uint32), ("geometry_ms", C.c_double), ("large_ms", C.c_double),
-                ("resolve_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+    _fields_ = [("draws", C.c_uint32), ("pad_", C.c_uint32), ("vertex_ms", C.c_double), ("geometry_ms", C.c_double),
+                ("large_ms", C.c_double), ("scan_ms", C.c_double), ("shade_ms", C.c_double),
+                ("clipped_ms", C.c_double), ("kernel_launches", C.c_uint64)]
 
 
 class DrawStats(C.Structure):

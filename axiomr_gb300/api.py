@@ -68,8 +68,9 @@ class Context:
             return None
         pr = _lib.Profile()
         check(self.lib.axr_profile_read(self.handle, C.byref(pr)), self.handle)
-        return {"draws": pr.draws, "geometry_ms": pr.geometry_ms, "large_ms": pr.large_ms,
-                "resolve_ms": pr.resolve_ms, "kernel_launches": pr.kernel_launches}
+        return {"draws": pr.draws, "vertex_ms": pr.vertex_ms, "geometry_ms": pr.geometry_ms,
+                "large_ms": pr.large_ms, "scan_ms": pr.scan_ms, "shade_ms": pr.shade_ms,
+                "clipped_ms": pr.clipped_ms, "kernel_launches": pr.kernel_launches}
 
     def close(self) -> None:
         if getattr(self, "handle", None):

@@ -62,11 +62,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     inc = [f"-I{ROOT / 'include'}", f"-I{CSRC}"]
     cu, cpp = _sources()
     logs = []
+    # tuning builds: e.g. AXR_NVCC_FLAGS="-DAXR_GEOMETRY_MIN_BLOCKS=6"
+    extra = os.environ.get("AXR_NVCC_FLAGS", "").split()
 
     def compile_cu(src: Path) -> Path:
         obj = objdir / (src.stem + ".cu.o")
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *inc, "-c", str(src), "-o", str(obj)]
+               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *inc, *extra, "-c", str(src), "-o", str(obj)]
         logs.append(_run(cmd))
         return obj
 

@@ -89,13 +89,12 @@ void free_scratch(axr_context* ctx) {
     dfree(ctx->large);
     dfree(ctx->items);
     dfree(ctx->vscreen);
-    dfree(ctx->vclip);
     dfree(ctx->vattr);
     dfree(ctx->shade);
     dfree(ctx->clip_px);
     ctx->large = nullptr;
     ctx->items = nullptr;
-    ctx->vscreen = ctx->vclip = ctx->vattr = nullptr;
+    ctx->vscreen = ctx->vattr = nullptr;
     ctx->shade = ctx->clip_px = nullptr;
     ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->px_cap = 0;
 }
@@ -124,7 +123,6 @@ axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uin
     AXR_CUDA(ctx, dmalloc(&ctx->large, want_tris));
     AXR_CUDA(ctx, dmalloc(&ctx->items, want_items));
     AXR_CUDA(ctx, dmalloc(&ctx->vscreen, want_verts));
-    AXR_CUDA(ctx, dmalloc(&ctx->vclip, want_verts));
     AXR_CUDA(ctx, dmalloc(&ctx->vattr, 4ull * want_verts));
     AXR_CUDA(ctx, dmalloc(&ctx->shade, want_px));
     AXR_CUDA(ctx, dmalloc(&ctx->clip_px, want_px));
@@ -196,7 +194,7 @@ DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffe
     p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
                          fb->width, fb->height, fb->tiles_x, fb->tiles_y};
     p.u = u;
-    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vscreen, ctx->vclip, ctx->vattr,
+    p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vscreen, ctx->vattr,
                            ctx->shade, ctx->clip_px, ctx->large_cap, ctx->item_cap, ctx->vcap, ctx->px_cap,
                            ctx->collect_stats, 0};
     p.small_max_pixels = ctx->small_max_pixels;
@@ -589,13 +587,13 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
     DrawParams p = make_params(ctx, mesh, ctx->fb, u);
     cudaEvent_t* ev = nullptr;
     if (ctx->profile && !ctx->capturing) {
-        while (ctx->event_pool.size() < ctx->events_used + 4) {
+        while (ctx->event_pool.size() < ctx->events_used + kStageEvents) {
             cudaEvent_t e;
             AXR_CUDA(ctx, cudaEventCreate(&e));
             ctx->event_pool.push_back(e);
         }
         ev = &ctx->event_pool[ctx->events_used];
-        ctx->events_used += 4;
+        ctx->events_used += kStageEvents;
     }
     AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, ev, &ctx->launches));
     return AXR_OK;
@@ -710,14 +708,13 @@ axr_status axr_profile_read(axr_context* ctx, axr_profile* out) {
     DeviceGuard g(ctx->device);
     AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     axr_profile r{};
-    for (size_t k = 0; k + 3 < ctx->events_used; k += 4) {
-        float a = 0, b = 0, c = 0;
-        AXR_CUDA(ctx, cudaEventElapsedTime(&a, ctx->event_pool[k], ctx->event_pool[k + 1]));
-        AXR_CUDA(ctx, cudaEventElapsedTime(&b, ctx->event_pool[k + 1], ctx->event_pool[k + 2]));
-        AXR_CUDA(ctx, cudaEventElapsedTime(&c, ctx->event_pool[k + 2], ctx->event_pool[k + 3]));
-        r.geometry_ms += a;
-        r.large_ms += b;
-        r.resolve_ms += c;
+    for (size_t k = 0; k + kStageEvents <= ctx->events_used; k += kStageEvents) {
+        double* out[6] = {&r.vertex_ms, &r.geometry_ms, &r.large_ms, &r.scan_ms, &r.shade_ms, &r.clipped_ms};
+        for (int j = 0; j < 6; ++j) {
+            float ms = 0.f;
+            AXR_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->event_pool[k + j], ctx->event_pool[k + j + 1]));
+            *out[j] += ms;
+        }
         ++r.draws;
     }
     ctx->events_used = 0;

@@ -73,7 +73,6 @@ struct axr_context {
     LargeTri* large = nullptr;
     LargeItem* items = nullptr;
     float4* vscreen = nullptr;
-    float4* vclip = nullptr;
     float4* vattr = nullptr;
     uint2* shade = nullptr;
     uint2* clip_px = nullptr;

@@ -115,7 +115,6 @@ constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh
 
 // Per-vertex cache written by the vertex pass of each draw:
 //   vscreen[i] = (screen x, screen y, NDC z, clip-plane masks as uint bits)
-//   vclip[i]   = clip-space position (mvp * (x, y, z, 1))
 //   vattr[n*i ...] = the shader's vertex outputs (n = VAttr<S>::n float4s)
 // Resolve work lists: shade[k] = (pixel index, depth-key tag) of every covered pixel of
 // the dirty tiles; clip_px[k] = the same pair for every pixel whose winner was clipped.
@@ -124,7 +123,6 @@ struct DevScratch {
     LargeTri* large;
     LargeItem* items;
     float4* vscreen;
-    float4* vclip;
     float4* vattr;
     uint2* shade;
     uint2* clip_px;

@@ -24,6 +24,8 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+// 1/x correctly rounded: the same bits as the IEEE division 1.0f / x.
+__device__ __forceinline__ float frcp(float a) { return __frcp_rn(a); }
 // std::max / std::min / std::clamp comparison semantics (NaN follows operator<)
 __device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
@@ -53,7 +55,7 @@ __device__ __forceinline__ f3 divs(f3 a, float s) { return {fdiv(a.x, s), fdiv(a
 __device__ __forceinline__ f3 subs(f3 a, float s) { return {fsub(a.x, s), fsub(a.y, s), fsub(a.z, s)}; }
 __device__ __forceinline__ f3 neg(f3 a) { return {-a.x, -a.y, -a.z}; }
 __device__ __forceinline__ float dot(f3 a, f3 b) { return fadd(fadd(fmul(a.x, b.x), fmul(a.y, b.y)), fmul(a.z, b.z)); }
-__device__ __forceinline__ f3 normalize(f3 v) { return mul(v, fdiv(1.0f, fsqrt(dot(v, v)))); }
+__device__ __forceinline__ f3 normalize(f3 v) { return mul(v, frcp(fsqrt(dot(v, v)))); }
 __device__ __forceinline__ f3 cross(f3 a, f3 b) {
     return {fsub(fmul(a.y, b.z), fmul(a.z, b.y)), fsub(fmul(a.z, b.x), fmul(a.x, b.z)),
             fsub(fmul(a.x, b.y), fmul(a.y, b.x))};

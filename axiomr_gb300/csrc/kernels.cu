@@ -41,6 +41,12 @@ namespace {
 constexpr int kBlock = 256;
 constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
+// Resident 256-thread CTAs per SM the geometry kernel is compiled for (register budget
+// 65536 / (256 * n)); 5 keeps it at 48 registers.
+#ifndef AXR_GEOMETRY_MIN_BLOCKS
+#define AXR_GEOMETRY_MIN_BLOCKS 5
+#endif
+
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
 
 // First writer of a tile in this draw appends it to the dirty-tile queue (at most one
@@ -60,7 +66,7 @@ __device__ __forceinline__ uint32_t tile_of(const DevTarget& t, int px, int py) 
 // Returns whether a key was written.
 __device__ __forceinline__ bool write_key(const DevTarget& t, int px, int py, float z, uint32_t tag) {
     if (!(z < __int_as_float(0x7f800000))) return false;  // +inf and NaN never pass early-Z
-    atomicMin(&t.key[(size_t)py * (size_t)t.width + (size_t)px], make_key(z, tag));
+    atomicMin(&t.key[(uint32_t)py * (uint32_t)t.width + (uint32_t)px], make_key(z, tag));
     return true;
 }
 
@@ -190,11 +196,10 @@ __global__ void __launch_bounds__(kBlock) vertex_kernel(const __grid_constant__ 
     f4 clip = mat4_mul(p.u.mvp, v.pos.x, v.pos.y, v.pos.z, 1.0f);
     f3 sc = screen_vertex(clip, (float)p.target.width, (float)p.target.height);
     p.scratch.vscreen[i] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(plane_masks(clip)));
-    p.scratch.vclip[i] = make_float4(clip.x, clip.y, clip.z, clip.w);
     pack_vsout<S>(vertex_shader<S>(p.u, v), &p.scratch.vattr[(size_t)VAttr<S>::n * i]);
 }
 
-__global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant__ DrawParams p) {
+__global__ void __launch_bounds__(kBlock, AXR_GEOMETRY_MIN_BLOCKS) geometry_kernel(const __grid_constant__ DrawParams p) {
     GeomStats st = {0, 0, 0};
     uint32_t single_tile = kNoTile;
     const uint32_t o = blockIdx.x * kBlock + threadIdx.x;
@@ -220,11 +225,9 @@ __global__ void __launch_bounds__(kBlock) geometry_kernel(const __grid_constant_
                     emit_triangle(p, s, o << 4, st, &single_tile);
                 } else if (cls < 0) {
                     CVClip a[kMaxClipVerts], b[kMaxClipVerts];
-                    const float4* vc = p.scratch.vclip;
-                    const float4 c0 = __ldg(&vc[f.x]), c1 = __ldg(&vc[f.y]), c2 = __ldg(&vc[f.z]);
-                    a[0].clip = mk4(c0.x, c0.y, c0.z, c0.w);
-                    a[1].clip = mk4(c1.x, c1.y, c1.z, c1.w);
-                    a[2].clip = mk4(c2.x, c2.y, c2.z, c2.w);
+                    a[0].clip = load_clip(p.mesh, p.u.mvp, f.x);
+                    a[1].clip = load_clip(p.mesh, p.u.mvp, f.y);
+                    a[2].clip = load_clip(p.mesh, p.u.mvp, f.z);
                     CVClip* out;
                     const int n = clip_triangle<0>(a, b, &out);
                     for (int j = 0; 3 * j + 2 < n; ++j) {
@@ -522,29 +525,34 @@ template <int S>
 cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream, cudaEvent_t* ev,
                           uint64_t* launches) {
     cudaError_t e;
+    auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], stream) : cudaSuccess; };
     if ((e = cudaMemsetAsync(p.scratch.counters, 0, kCountersReset, stream)) != cudaSuccess) return e;
-    if (ev && (e = cudaEventRecord(ev[0], stream)) != cudaSuccess) return e;
+    if ((e = mark(0)) != cudaSuccess) return e;
     if (p.mesh.num_drawn > 0) {
         vertex_kernel<S><<<grid_for(p.mesh.num_vertices, kBlock, 0x7FFFFFFFu), kBlock, 0, stream>>>(p);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = mark(1)) != cudaSuccess) return e;
         geometry_kernel<<<grid_for(p.mesh.num_drawn, kBlock, 0x7FFFFFFFu), kBlock, 0, stream>>>(p);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         *launches += 2;
+    } else if ((e = mark(1)) != cudaSuccess) {
+        return e;
     }
-    if (ev && (e = cudaEventRecord(ev[1], stream)) != cudaSuccess) return e;
+    if ((e = mark(2)) != cudaSuccess) return e;
     large_kernel<<<(unsigned)(cfg.num_sms * cfg.large_ctas_per_sm), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (ev && (e = cudaEventRecord(ev[2], stream)) != cudaSuccess) return e;
+    if ((e = mark(3)) != cudaSuccess) return e;
     const unsigned tiles = (unsigned)(p.target.tiles_x * p.target.tiles_y);
     scan_kernel<<<min((tiles + 7u) / 8u, (unsigned)(cfg.num_sms * 8)), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = mark(4)) != cudaSuccess) return e;
     shade_kernel<S><<<(unsigned)(cfg.num_sms * cfg.resolve_ctas_per_sm), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = mark(5)) != cudaSuccess) return e;
     resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms, kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *launches += 4;
-    if (ev) return cudaEventRecord(ev[3], stream);
-    return cudaSuccess;
+    return mark(6);
 }
 
 }  // namespace

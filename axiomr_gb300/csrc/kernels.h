@@ -15,8 +15,10 @@ struct LaunchConfig {
 
 // One draw: geometry (transform, clip, cull, setup, small-triangle raster) -> large
 // triangle tile raster -> per-tile resolve and shading into the framebuffer.
-// `stage_events` (optional, 4 events) are recorded before the geometry kernel and after
-// each of the three kernels. Adds the number of kernels launched to *launches.
+// `stage_events` (optional, kStageEvents events) are recorded before the first kernel and
+// after each of the six (vertex, geometry, large, scan, shade, clipped). Adds the number
+// of kernels launched to *launches.
+constexpr int kStageEvents = 7;
 cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream,
                         cudaEvent_t* stage_events, uint64_t* launches);
 

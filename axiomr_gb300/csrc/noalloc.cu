@@ -13,7 +13,7 @@
 //
 // Limits: at most kNoAllocMaxVertices vertices, kNoAllocMaxFaces drawn faces and
 // kNoAllocMaxPixels framebuffer pixels per call; larger draws are rejected with
-// AXR_E_CAPACITY. The array (about 28 MiB) is reserved on every GPU that loads the library
+// AXR_E_CAPACITY. The array (about 27 MiB) is reserved on every GPU that loads the library
 // and stays reserved until the process exits.
 //
 // Set-up: the first call on each device looks up the array's device address with
@@ -39,8 +39,7 @@ constexpr size_t kOffCounters = 0;
 constexpr size_t kOffLarge = align256(kOffCounters + sizeof(axr::DevCounters));
 constexpr size_t kOffItems = align256(kOffLarge + sizeof(axr::LargeTri) * kNoAllocMaxFaces);
 constexpr size_t kOffVscreen = align256(kOffItems + sizeof(axr::LargeItem) * kNoAllocMaxItems);
-constexpr size_t kOffVclip = align256(kOffVscreen + sizeof(float4) * kNoAllocMaxVertices);
-constexpr size_t kOffVattr = align256(kOffVclip + sizeof(float4) * kNoAllocMaxVertices);
+constexpr size_t kOffVattr = align256(kOffVscreen + sizeof(float4) * kNoAllocMaxVertices);
 constexpr size_t kOffShade = align256(kOffVattr + 4 * sizeof(float4) * kNoAllocMaxVertices);
 constexpr size_t kOffClip = align256(kOffShade + sizeof(uint2) * kNoAllocMaxPixels);
 constexpr size_t kNoAllocBytes = align256(kOffClip + sizeof(uint2) * kNoAllocMaxPixels);
@@ -105,7 +104,6 @@ extern "C" axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* me
                                reinterpret_cast<LargeTri*>(base + kOffLarge),
                                reinterpret_cast<LargeItem*>(base + kOffItems),
                                reinterpret_cast<float4*>(base + kOffVscreen),
-                               reinterpret_cast<float4*>(base + kOffVclip),
                                reinterpret_cast<float4*>(base + kOffVattr),
                                reinterpret_cast<uint2*>(base + kOffShade),
                                reinterpret_cast<uint2*>(base + kOffClip),

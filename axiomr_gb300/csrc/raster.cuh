@@ -163,7 +163,7 @@ __device__ __forceinline__ float clamp_w(float w) {
 
 // Screen position and NDC depth of one clip-space vertex (Triangle ctor, per vertex).
 __device__ __forceinline__ f3 screen_vertex(f4 c, float fw, float fh) {
-    float inv = fdiv(1.0f, clamp_w(c.w));
+    float inv = frcp(clamp_w(c.w));
     return mk3(fmul(fmul(fadd(fmul(c.x, inv), 1.0f), 0.5f), fw), fmul(fmul(fadd(fmul(c.y, inv), 1.0f), 0.5f), fh),
                fmul(c.z, inv));
 }
@@ -265,7 +265,7 @@ __device__ __forceinline__ bool edge_setup(const Screen& s, int width, int heigh
     e.a[0] = a0; e.b[0] = b0; e.c[0] = c0;
     e.a[1] = a1; e.b[1] = b1; e.c[1] = c1;
     e.a[2] = a2; e.b[2] = b2; e.c[2] = c2;
-    e.inv_area = fdiv(1.0f, area);
+    e.inv_area = frcp(area);
     e.z[0] = s.z[0]; e.z[1] = s.z[1]; e.z[2] = s.z[2];
     return true;
 }

@@ -235,7 +235,7 @@ __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMat
         float denom = fadd(fmul(fmul(4.0f, ndotv), ndotl), 0.0001f);
         f3 specular = divs(numerator, denom);
         f3 kd = mul(sub(one, f), one_minus_metallic);
-        f3 diffuse = mul(mul(kd, albedo), fdiv(1.0f, pi));
+        f3 diffuse = mul(mul(kd, albedo), frcp(pi));
         f3 ambient = mul(mul(mk3(0.03f, 0.03f, 0.03f), albedo), ao);
         f3 c = add(ambient, mul(mul(add(diffuse, specular), lc), ndotl));
         c = div(c, add(c, one));

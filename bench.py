@@ -363,21 +363,30 @@ def run_ours(args, dist: Dist):
 
     # ---- roofline of the dominant kernel
     n = max(1, prof["draws"])
-    stage_us = {"geometry": prof["geometry_ms"] / n * 1e3, "large": prof["large_ms"] / n * 1e3,
-                "resolve": prof["resolve_ms"] / n * 1e3}
+    stages = ("vertex", "geometry", "large", "scan", "shade", "clipped")
+    stage_us = {k: prof[k + "_ms"] / n * 1e3 for k in stages}
     V, F = m.num_vertices, m.num_faces
     P = scene.width * scene.height
     frags = st["fragments"]
-    resolved_px = min(P, st["tiles"] * 256)
+    scanned_px = min(P, st["tiles"] * 256)
+    vattr = {W.SHADER_PHONG: 64, W.SHADER_PBR: 64, W.SHADER_BLINN_PHONG: 32}.get(shader_kind, 16)
+    vin = 40 + (24 if need_tbn else 0)  # position, normal, uv (+ tangent, bitangent) read per vertex
     algo_bytes = {
-        # indices + positions read once, one 8-byte depth-key write per covered fragment
-        "geometry": 12.0 * F + 12.0 * V + 8.0 * frags,
+        # vertex attributes read once, screen cache (16 B) + shader outputs written once
+        "vertex": float(V) * (vin + 16 + vattr),
+        # indices read once, cached screen positions read once per vertex, one 8-byte
+        # depth-key write per covered fragment
+        "geometry": 12.0 * F + 16.0 * V + 8.0 * frags,
         "large": 8.0 * frags,
-        # per resolved pixel: key read + reset, depth read, colour + depth write; vertex
-        # attributes (position, uv, normal) once
-        "resolve": 28.0 * resolved_px + 32.0 * V,
+        # keys of the dirty tiles read, one 8-byte work entry per covered pixel written
+        "scan": 8.0 * scanned_px + 8.0 * frags,
+        # per covered pixel: work entry, indices, depth read, colour + depth write; the
+        # vertex cache read once
+        "shade": frags * (8.0 + 12.0 + 4.0 + 8.0) + float(V) * (16 + vattr),
+        "clipped": 0.0,
     }
-    kernel_names = {"geometry": "geometry_kernel", "large": "large_kernel", "resolve": "resolve_kernel"}
+    kernel_names = {k: k + "_kernel" for k in stages}
+    kernel_names["clipped"] = "resolve_clipped_kernel"
     dom = max(stage_us, key=stage_us.get)
     hbm_peak, peak_kind = measured_peaks()
     achieved = algo_bytes[dom] / (stage_us[dom] * 1e-6) / 1e9

@@ -190,7 +190,7 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
 /* No counterpart in the reference. The same draw as axr_draw_mesh for callers that cannot
  * allocate device memory: a renderer recording its frame into a CUDA graph, a real-time
  * loop that forbids allocator calls after start-up, or a host that owns the device-memory
- * budget. Its scratch lives in one fixed device array inside the library (about 28 MiB,
+ * budget. Its scratch lives in one fixed device array inside the library (about 27 MiB,
  * reserved on every GPU that loads the library until exit), so the call allocates nothing.
  * Limits: 65536 vertices, 65536 drawn faces, 1024*1024 framebuffer pixels; larger draws
  * return AXR_E_CAPACITY. The first call on a device looks up the array's address, so make
@@ -249,9 +249,12 @@ axr_status axr_stats_read(axr_context* ctx, axr_draw_stats* out); /* synchronise
 typedef struct axr_profile {
     uint32_t draws;          /* draws recorded */
     uint32_t pad_;
-    double geometry_ms;      /* transform, clip, cull, setup, small-triangle raster */
+    double vertex_ms;        /* per-vertex transform and vertex shader */
+    double geometry_ms;      /* clip, cull, setup, small-triangle raster */
     double large_ms;         /* large-triangle tile raster */
-    double resolve_ms;       /* per-tile resolve and shading */
+    double scan_ms;          /* dirty-tile key scan */
+    double shade_ms;         /* per-pixel resolve and shading */
+    double clipped_ms;       /* resolve of pixels won by clipped triangles */
     uint64_t kernel_launches;/* all kernels launched on this context since creation */
 } axr_profile;
 axr_status axr_profile_enable(axr_context* ctx, int32_t enable);
