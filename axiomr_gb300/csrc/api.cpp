@@ -191,7 +191,7 @@ DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffe
     DrawParams p{};
     p.mesh = DevMesh{m->pos, m->nrm, m->tan, m->bit, m->uv, m->idx, m->groups, m->materials,
                      m->num_vertices, m->num_faces, m->num_groups, m->num_drawn};
-    p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
+    p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag,
                          fb->width, fb->height, fb->tiles_x, fb->tiles_y};
     p.u = u;
     p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vscreen, ctx->vattr,
@@ -227,11 +227,17 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
                     prop.major, prop.minor);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, sizeof(DevCounters));
     if (e != cudaSuccess) {
         axr_status st = cuda_fail(nullptr, e, "context setup");
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+        if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
+        if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
+        if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
         dfree(ctx->counters);
         delete ctx;
         return st;
@@ -251,6 +257,10 @@ void axr_context_destroy(axr_context* ctx) {
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     dfree(ctx->counters);
     free_scratch(ctx);
+    if (ctx->aux.stream) cudaStreamSynchronize(ctx->aux.stream);
+    if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
+    if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
+    if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -450,14 +460,13 @@ axr_status axr_framebuffer_create(axr_context* ctx, int32_t width, int32_t heigh
     if (e == cudaSuccess) e = dmalloc(&fb->depth, n);
     if (e == cudaSuccess) e = dmalloc(&fb->key, n);
     if (e == cudaSuccess) e = dmalloc(&fb->tile_flag, nt);
-    if (e == cudaSuccess) e = dmalloc(&fb->tile_queue, nt);
     if (e == cudaSuccess) e = cudaMemsetAsync(fb->tile_flag, 0, nt * 4, ctx->stream);
     if (e == cudaSuccess) e = launch_fill_u64(fb->key, n, kEmptyKey, ctx->stream);
     // Framebuffer(w, h, true): colour 0, depth +inf (src/framebuffer.cpp:6-14)
     if (e == cudaSuccess) e = launch_clear(fb->color, fb->depth, n, 0u, INFINITY, true, true, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
-        dfree(fb->color); dfree(fb->depth); dfree(fb->key); dfree(fb->tile_flag); dfree(fb->tile_queue);
+        dfree(fb->color); dfree(fb->depth); dfree(fb->key); dfree(fb->tile_flag);
         delete fb;
         return cuda_fail(ctx, e, "framebuffer allocation");
     }
@@ -470,7 +479,7 @@ void axr_framebuffer_destroy(axr_context* ctx, axr_framebuffer* fb) {
     DeviceGuard g(fb->device);
     if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx && ctx->fb == fb) ctx->fb = nullptr;
-    dfree(fb->color); dfree(fb->depth); dfree(fb->key); dfree(fb->tile_flag); dfree(fb->tile_queue);
+    dfree(fb->color); dfree(fb->depth); dfree(fb->key); dfree(fb->tile_flag);
     delete fb;
 }
 
@@ -595,7 +604,7 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
         ev = &ctx->event_pool[ctx->events_used];
         ctx->events_used += kStageEvents;
     }
-    AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, ev, &ctx->launches));
+    AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, &ctx->aux, ev, &ctx->launches));
     return AXR_OK;
 }
 

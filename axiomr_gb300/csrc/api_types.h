@@ -45,7 +45,6 @@ struct axr_framebuffer {
     float* depth = nullptr;
     unsigned long long* key = nullptr;
     uint32_t* tile_flag = nullptr;
-    uint32_t* tile_queue = nullptr;
     int32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
     int device = 0;
 };
@@ -59,6 +58,7 @@ struct axr_context {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+    axr::AuxStream aux{};  // side stream + fork/join events for the clipped-winner pass
     LaunchConfig cfg{};
     std::mutex mu;
     std::string error;

@@ -10,7 +10,8 @@
 // Texture: RGBA8 texels, row 0 first (as stbi_load returns them), one uint32 per texel.
 // Framebuffer: color[W*H] uint32 holding B,G,R,A bytes (row 0 = bottom, reference
 //   include/framebuffer.hpp:14-21), depth[W*H] float, key[W*H] uint64 (depth|order
-//   visibility keys, all-ones between draws), tile_flag[TX*TY] uint32, tile_queue[TX*TY].
+//   visibility keys, all-ones between draws), tile_flag[TX*TY] uint32 (16x16 tile holds a
+//   key; set by the rasterisers, cleared by the key scan).
 #pragma once
 #include <stdint.h>
 #include <vector_types.h>
@@ -59,7 +60,6 @@ struct DevTarget {
     float* depth;
     unsigned long long* key;
     uint32_t* tile_flag;
-    uint32_t* tile_queue;
     int32_t width, height, tiles_x, tiles_y;
 };
 
@@ -98,10 +98,9 @@ struct DevCounters {
     uint32_t large_count;     // LargeTri slots reserved (may exceed the capacity)
     uint32_t item_count;      // LargeItem slots reserved (may exceed the capacity)
     uint32_t item_head;       // next LargeItem to hand out
-    uint32_t queue_len;       // dirty tiles appended
-    uint32_t clip_count;      // pixels whose winner is a clipped triangle (second resolve pass)
-    uint32_t shade_count;     // covered pixels found by the key scan
-    uint32_t pad_;
+    uint32_t shade_count;     // covered pixels (unclipped winners) found by the key scan
+    uint32_t clip_count;      // covered pixels whose winner is a clipped triangle
+    uint32_t pad_[2];
     uint32_t error;           // sticky error bits (kErr*), cleared by axr_sync
     unsigned long long stat_triangles;   // triangles that passed clip + cull
     unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
@@ -109,15 +108,16 @@ struct DevCounters {
     unsigned long long stat_tiles;       // dirty tiles resolved
 };
 
-constexpr unsigned kCountersReset = 6 * sizeof(uint32_t);
+constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
 constexpr uint32_t kErrOrdinal = 1u;  // more faces than a depth key can order
 constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh (face skipped)
 
 // Per-vertex cache written by the vertex pass of each draw:
 //   vscreen[i] = (screen x, screen y, NDC z, clip-plane masks as uint bits)
 //   vattr[n*i ...] = the shader's vertex outputs (n = VAttr<S>::n float4s)
-// Resolve work lists: shade[k] = (pixel index, depth-key tag) of every covered pixel of
-// the dirty tiles; clip_px[k] = the same pair for every pixel whose winner was clipped.
+// Resolve work lists written by the key scan: shade[k] = (pixel index, depth-key tag) of a
+// covered pixel whose winner is an unclipped triangle; clip_px[k] = the same pair when the
+// winner came out of the clipper.
 struct DevScratch {
     DevCounters* counters;
     LargeTri* large;

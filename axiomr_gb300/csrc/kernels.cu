@@ -15,8 +15,8 @@
 //                    record and one work item per 16x16 tile of their box.
 //   large_kernel     warps take tile work items (4 per atomic) and evaluate 256 pixels
 //                    each, 8 per lane.
-//   scan_kernel      one warp per dirty 16x16 tile: compacts the tile's covered pixels
-//                    (non-empty depth keys) into a shade list and resets the keys.
+//   scan_kernel      one warp per flagged 16x16 tile: compacts the tile's covered pixels
+//                    (non-empty depth keys) into the shade / clipped lists, resets the keys.
 //   shade_kernel     one thread per covered pixel: the winner is re-derived from its depth
 //                    key, shaded once, and merged into the framebuffer with the reference's
 //                    strict less-than test (winners that were clipped go to
@@ -49,14 +49,9 @@ constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
 
-// First writer of a tile in this draw appends it to the dirty-tile queue (at most one
-// entry per tile per draw, so the queue never exceeds tiles_x * tiles_y).
-__device__ __forceinline__ void mark_tile(const DevTarget& t, DevCounters* c, uint32_t tile) {
-    if (ld_volatile(&t.tile_flag[tile]) == 0u && atomicExch(&t.tile_flag[tile], 1u) == 0u) {
-        uint32_t q = atomicAdd(&c->queue_len, 1u);
-        t.tile_queue[q] = tile;
-    }
-}
+// A tile that holds at least one depth key is flagged for the key scan (a plain store:
+// every writer stores the same value).
+__device__ __forceinline__ void mark_tile(const DevTarget& t, uint32_t tile) { t.tile_flag[tile] = 1u; }
 
 __device__ __forceinline__ uint32_t tile_of(const DevTarget& t, int px, int py) {
     return (uint32_t)(py >> 4) * (uint32_t)t.tiles_x + (uint32_t)(px >> 4);
@@ -121,10 +116,10 @@ __device__ __forceinline__ uint32_t tiles_of(const Edges& e, uint32_t& ntx) {
     return ntx * (uint32_t)(ty1 - ty0 + 1);
 }
 
-__device__ void mark_box(const DevTarget& t, DevCounters* c, const Edges& e) {
+__device__ void mark_box(const DevTarget& t, const Edges& e) {
     for (int ty = e.y_lo >> 4; ty <= (e.y_hi - 1) >> 4; ++ty)
         for (int tx = e.x_lo >> 4; tx <= (e.x_hi - 1) >> 4; ++tx)
-            mark_tile(t, c, (uint32_t)ty * (uint32_t)t.tiles_x + (uint32_t)tx);
+            mark_tile(t, (uint32_t)ty * (uint32_t)t.tiles_x + (uint32_t)tx);
 }
 
 __device__ __forceinline__ void store_large(LargeTri* dst, const Edges& e, uint32_t tag) {
@@ -167,7 +162,7 @@ __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag
             if (tiles_of(e, ntx) == 1u && *single_tile == kNoTile)
                 *single_tile = tile_of(p.target, e.x_lo, e.y_lo);
             else
-                mark_box(p.target, c, e);
+                mark_box(p.target, e);
         }
         return;
     }
@@ -183,7 +178,7 @@ __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag
     } else {
         // lists full: mark the reserved items empty and rasterise the triangle here
         for (uint32_t k = base; k < icap && k - base < nt; ++k) p.scratch.items[k] = LargeItem{kNoItem, 0u};
-        if (raster_box(p.target, e, tag, st)) mark_box(p.target, c, e);
+        if (raster_box(p.target, e, tag, st)) mark_box(p.target, e);
     }
 }
 
@@ -236,7 +231,7 @@ __global__ void __launch_bounds__(kBlock, AXR_GEOMETRY_MIN_BLOCKS) geometry_kern
                                      p.target.height, s);
                         uint32_t tile = kNoTile;
                         emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile);
-                        if (tile != kNoTile) mark_tile(p.target, p.scratch.counters, tile);
+                        if (tile != kNoTile) mark_tile(p.target, tile);
                     }
                 }
             }
@@ -245,7 +240,7 @@ __global__ void __launch_bounds__(kBlock, AXR_GEOMETRY_MIN_BLOCKS) geometry_kern
     // one mark per distinct tile in the warp
     const unsigned peers = __match_any_sync(0xFFFFFFFFu, single_tile);
     if (single_tile != kNoTile && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1))
-        mark_tile(p.target, p.scratch.counters, single_tile);
+        mark_tile(p.target, single_tile);
     if (p.scratch.collect_stats) {
         const unsigned full = 0xFFFFFFFFu;
         uint32_t t = __reduce_add_sync(full, st.tris), fr = __reduce_add_sync(full, st.frags);
@@ -296,7 +291,7 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
                 }
             }
             if (__any_sync(0xFFFFFFFFu, wrote) && lane == 0)
-                mark_tile(p.target, c, (uint32_t)ty * (uint32_t)p.target.tiles_x + (uint32_t)tx);
+                mark_tile(p.target, (uint32_t)ty * (uint32_t)p.target.tiles_x + (uint32_t)tx);
         }
     }
     if (p.scratch.collect_stats) {
@@ -305,52 +300,82 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
     }
 }
 
-// Key scan: one warp per dirty tile (grid-stride over the tile queue) reads the tile's 256
-// keys, 8 per lane, appends (pixel, tag) of every covered pixel to the shade list
-// (warp-aggregated), resets those keys and clears the tile flag.
+// Key scan over every tile of the target, one warp per tile and 8 tiles per CTA round:
+// flagged tiles have their 256 keys read (8 per lane), every covered pixel is appended as
+// (pixel, tag) to the shade list, or to the clipped list when its winner came out of the
+// clipper, and the keys and the flag are reset. List space is taken once per CTA round
+// (shared-memory prefix over the 8 warps), so the global counters see few atomics.
 __global__ void __launch_bounds__(kBlock) scan_kernel(const __grid_constant__ DrawParams p) {
+    constexpr int kWarps = kBlock / 32;
+    __shared__ uint32_t s_count[2][kWarps];
+    __shared__ uint32_t s_base[2];
     DevCounters* c = p.scratch.counters;
     const DevTarget& t = p.target;
-    const uint32_t qlen = ld_volatile(&c->queue_len);
-    const int lane = threadIdx.x & 31;
-    const uint32_t nwarps = gridDim.x * (kBlock / 32);
-    for (uint32_t q = blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); q < qlen; q += nwarps) {
-        const uint32_t tile = t.tile_queue[q];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const uint32_t ntiles = (uint32_t)t.tiles_x * (uint32_t)t.tiles_y;
+    for (uint32_t first = blockIdx.x * kWarps; first < ntiles; first += gridDim.x * kWarps) {
+        const uint32_t tile = first + (uint32_t)warp;
+        const bool dirty = tile < ntiles && ld_volatile(&t.tile_flag[tile]) != 0u;
         const int px = (int)(tile % (uint32_t)t.tiles_x) * kTile + (lane & 15);
         const int py0 = (int)(tile / (uint32_t)t.tiles_x) * kTile + (lane >> 4);
         unsigned long long keys[8];
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int py = py0 + 2 * r;
-            keys[r] = (px < t.width && py < t.height) ? t.key[(size_t)py * (size_t)t.width + (size_t)px] : kEmptyKey;
-        }
-        // one atomic per tile: per-row ballots give each covered pixel its slot
-        unsigned m[8];
-        uint32_t total = 0;
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            m[r] = __ballot_sync(0xFFFFFFFFu, keys[r] != kEmptyKey);
-            total += (uint32_t)__popc(m[r]);
-        }
-        if (total != 0u) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(&c->shade_count, total);
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            const unsigned below = (1u << lane) - 1u;
+        unsigned ms[8], mc[8];
+        uint32_t ns = 0, nc = 0;
+        if (dirty) {
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-                if (keys[r] != kEmptyKey) {
-                    const uint32_t idx = (uint32_t)((size_t)(py0 + 2 * r) * (size_t)t.width + (size_t)px);
-                    p.scratch.shade[base + (uint32_t)__popc(m[r] & below)] = make_uint2(idx, (uint32_t)keys[r]);
-                    t.key[idx] = kEmptyKey;
-                }
-                base += (uint32_t)__popc(m[r]);
+                const int py = py0 + 2 * r;
+                keys[r] = (px < t.width && py < t.height) ? t.key[(uint32_t)py * (uint32_t)t.width + (uint32_t)px]
+                                                          : kEmptyKey;
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const bool has = keys[r] != kEmptyKey;
+                const bool clipped = has && (((uint32_t)keys[r]) & 8u) != 0u;
+                ms[r] = __ballot_sync(0xFFFFFFFFu, has && !clipped);
+                mc[r] = __ballot_sync(0xFFFFFFFFu, clipped);
+                ns += (uint32_t)__popc(ms[r]);
+                nc += (uint32_t)__popc(mc[r]);
             }
         }
         if (lane == 0) {
-            t.tile_flag[tile] = 0u;
-            if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
+            s_count[0][warp] = ns;
+            s_count[1][warp] = nc;
         }
+        __syncthreads();
+        if (threadIdx.x < 2) {
+            uint32_t total = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                const uint32_t v = s_count[threadIdx.x][w];
+                s_count[threadIdx.x][w] = total;
+                total += v;
+            }
+            s_base[threadIdx.x] = total ? atomicAdd(threadIdx.x == 0 ? &c->shade_count : &c->clip_count, total) : 0u;
+        }
+        __syncthreads();
+        if (dirty) {
+            uint32_t bs = s_base[0] + s_count[0][warp], bc = s_base[1] + s_count[1][warp];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                if (keys[r] != kEmptyKey) {
+                    const uint32_t idx = (uint32_t)(py0 + 2 * r) * (uint32_t)t.width + (uint32_t)px;
+                    const uint2 entry = make_uint2(idx, (uint32_t)keys[r]);
+                    if ((uint32_t)keys[r] & 8u)
+                        p.scratch.clip_px[bc + (uint32_t)__popc(mc[r] & below)] = entry;
+                    else
+                        p.scratch.shade[bs + (uint32_t)__popc(ms[r] & below)] = entry;
+                    t.key[idx] = kEmptyKey;
+                }
+                bs += (uint32_t)__popc(ms[r]);
+                bc += (uint32_t)__popc(mc[r]);
+            }
+            if (lane == 0) {
+                t.tile_flag[tile] = 0u;
+                if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -368,10 +393,9 @@ __device__ __forceinline__ void shade_winner(const DrawParams& p, size_t idx, in
     t.depth[idx] = r.z;
 }
 
-// Dense shading of the covered pixels: the winner is re-derived from its tag (face ->
-// cached vertex screen positions and shader outputs), its barycentrics recomputed exactly
-// and the fragment shaded once. Winners that came out of the clipper go to the clipped
-// list (resolve_clipped_kernel).
+// Dense shading of the covered pixels whose winner is unclipped: the winner is re-derived
+// from its tag (face -> cached vertex screen positions and shader outputs), its
+// barycentrics recomputed exactly and the fragment shaded once.
 template <int S>
 __global__ void __launch_bounds__(kBlock) shade_kernel(const __grid_constant__ DrawParams p) {
     DevCounters* c = p.scratch.counters;
@@ -380,11 +404,6 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const __grid_constant__ D
     for (uint32_t q = blockIdx.x * kBlock + threadIdx.x; q < n; q += gridDim.x * kBlock) {
         const uint2 w = p.scratch.shade[q];
         const uint32_t tag = w.y;
-        if (tag & 8u) {
-            const uint32_t slot = atomicAdd(&c->clip_count, 1u);
-            p.scratch.clip_px[slot] = w;  // at most one entry per pixel: slot < px_cap
-            continue;
-        }
         const size_t idx = w.x;
         const int px = (int)(idx % (size_t)t.width), py = (int)(idx / (size_t)t.width);
         const FaceRef fr = face_of(p.mesh, tag >> 4);
@@ -522,8 +541,8 @@ unsigned grid_for(size_t n, int block, unsigned cap = 65535u * 16u) {
 }
 
 template <int S>
-cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream, cudaEvent_t* ev,
-                          uint64_t* launches) {
+cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream, const AuxStream* aux,
+                          cudaEvent_t* ev, uint64_t* launches) {
     cudaError_t e;
     auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], stream) : cudaSuccess; };
     if ((e = cudaMemsetAsync(p.scratch.counters, 0, kCountersReset, stream)) != cudaSuccess) return e;
@@ -546,25 +565,35 @@ cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStre
     scan_kernel<<<min((tiles + 7u) / 8u, (unsigned)(cfg.num_sms * 8)), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = mark(4)) != cudaSuccess) return e;
+    // the clipped-winner pass is independent of the main shading pass: run it beside it
+    cudaStream_t side = aux ? aux->stream : stream;
+    if (aux) {
+        if ((e = cudaEventRecord(aux->fork, stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) return e;
+    }
+    resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms / 2u + 1u, kBlock, 0, side>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     shade_kernel<S><<<(unsigned)(cfg.num_sms * cfg.resolve_ctas_per_sm), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = mark(5)) != cudaSuccess) return e;
-    resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms, kBlock, 0, stream>>>(p);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (aux) {
+        if ((e = cudaEventRecord(aux->join, aux->stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(stream, aux->join, 0)) != cudaSuccess) return e;
+    }
     *launches += 4;
     return mark(6);
 }
 
 }  // namespace
 
-cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream,
+cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream, const AuxStream* aux,
                         cudaEvent_t* stage_events, uint64_t* launches) {
     switch (p.u.shader) {
-        case kFlat: return launch_shaded<kFlat>(p, cfg, stream, stage_events, launches);
-        case kPhong: return launch_shaded<kPhong>(p, cfg, stream, stage_events, launches);
-        case kPBR: return launch_shaded<kPBR>(p, cfg, stream, stage_events, launches);
-        case kBlinnPhong: return launch_shaded<kBlinnPhong>(p, cfg, stream, stage_events, launches);
-        case kGouraud: return launch_shaded<kGouraud>(p, cfg, stream, stage_events, launches);
+        case kFlat: return launch_shaded<kFlat>(p, cfg, stream, aux, stage_events, launches);
+        case kPhong: return launch_shaded<kPhong>(p, cfg, stream, aux, stage_events, launches);
+        case kPBR: return launch_shaded<kPBR>(p, cfg, stream, aux, stage_events, launches);
+        case kBlinnPhong: return launch_shaded<kBlinnPhong>(p, cfg, stream, aux, stage_events, launches);
+        case kGouraud: return launch_shaded<kGouraud>(p, cfg, stream, aux, stage_events, launches);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -7,6 +7,13 @@
 
 namespace axr {
 
+// Side stream and events of a context: the clipped-winner resolve pass runs on the side
+// stream, concurrently with the main shading pass (fork after the key scan, join after).
+struct AuxStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
+
 struct LaunchConfig {
     int num_sms;
     int large_ctas_per_sm;
@@ -19,7 +26,7 @@ struct LaunchConfig {
 // after each of the six (vertex, geometry, large, scan, shade, clipped). Adds the number
 // of kernels launched to *launches.
 constexpr int kStageEvents = 7;
-cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream,
+cudaError_t launch_draw(const DrawParams& p, const LaunchConfig& cfg, cudaStream_t stream, const AuxStream* aux,
                         cudaEvent_t* stage_events, uint64_t* launches);
 
 cudaError_t launch_clear(uint32_t* color, float* depth, size_t pixels, uint32_t bgra, float depth_value,

@@ -96,7 +96,7 @@ extern "C" axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* me
         DrawParams p{};
         p.mesh = DevMesh{mesh->pos, mesh->nrm, mesh->tan, mesh->bit, mesh->uv, mesh->idx, mesh->groups,
                          mesh->materials, mesh->num_vertices, mesh->num_faces, mesh->num_groups, mesh->num_drawn};
-        p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag, fb->tile_queue,
+        p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag,
                              fb->width, fb->height, fb->tiles_x, fb->tiles_y};
         p.u = make_uniforms(ctx->camera, ctx->shader, model);
         DevCounters* counters = reinterpret_cast<DevCounters*>(base + kOffCounters);
@@ -112,7 +112,7 @@ extern "C" axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* me
         p.small_max_pixels = ctx->small_max_pixels;
         // the array keeps the previous call's contents: start from zeroed counters
         e = cudaMemsetAsync(counters, 0, sizeof(DevCounters), ctx->stream);
-        if (e == cudaSuccess) e = launch_draw(p, ctx->cfg, ctx->stream, nullptr, &ctx->launches);
+        if (e == cudaSuccess) e = launch_draw(p, ctx->cfg, ctx->stream, &ctx->aux, nullptr, &ctx->launches);
     }
     if (prev >= 0 && prev != ctx->device) cudaSetDevice(prev);
     if (e != cudaSuccess) return noalloc_fail(ctx, AXR_E_CUDA, std::string("axr_draw_mesh_noalloc: ") + cudaGetErrorString(e));
