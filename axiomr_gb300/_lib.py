@@ -46,15 +46,28 @@ class CameraDesc(C.Structure):
     _fields_ = [("view_proj", C.c_float * 16), ("viewport", C.c_float * 16), ("position", C.c_float * 3)]
 
 
+AXR_DRAW_CLEAR_COLOR = 1
+AXR_DRAW_CLEAR_DEPTH = 2
+AXR_TUNE_CLASSES = 6
+
+
 class DrawDesc(C.Structure):
     _fields_ = [("mesh", C.c_void_p), ("framebuffer", C.c_void_p), ("model", C.c_float * 16),
-                ("camera", CameraDesc), ("shader", ShaderDesc)]
+                ("camera", CameraDesc), ("shader", ShaderDesc), ("clear_flags", C.c_uint32),
+                ("clear_rgba", C.c_uint8 * 4), ("clear_depth", C.c_float)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("draws", C.c_uint32), ("launches", C.c_uint32), ("vertices", C.c_uint64), ("faces", C.c_uint64),
+                ("pixels", C.c_uint64), ("tiles", C.c_uint64), ("device_bytes", C.c_uint64)]
 
 
 class Profile(C.Structure):
     _fields_ = [("draws", C.c_uint32), ("pad_", C.c_uint32), ("vertex_ms", C.c_double), ("geometry_ms", C.c_double),
                 ("large_ms", C.c_double), ("scan_ms", C.c_double), ("shade_ms", C.c_double),
-                ("clipped_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+                ("clipped_ms", C.c_double), ("kernel_launches", C.c_uint64), ("batch_launches", C.c_uint64),
+                ("batch_vertex_ms", C.c_double), ("batch_face_ms", C.c_double), ("batch_large_ms", C.c_double),
+                ("batch_tile_ms", C.c_double)]
 
 
 class DrawStats(C.Structure):
@@ -98,7 +111,15 @@ SIGNATURES = {
     "axr_set_framebuffer": (S, [P, P]),
     "axr_draw_mesh": (S, [P, P, P]),
     "axr_draw_mesh_noalloc": (S, [P, P, P]),
+    "axr_batch_create": (S, [P, P, C.c_int32, PP]),
+    "axr_batch_launch": (S, [P, P]),
+    "axr_batch_destroy": (None, [P, P]),
+    "axr_batch_get_info": (S, [P, P]),
     "axr_draw_batch": (S, [P, P, C.c_int32]),
+    "axr_batch_autotune": (S, [P, P, C.c_int32, C.c_int32, P]),
+    "axr_batch_get_tuning": (S, [P, P]),
+    "axr_batch_set_tuning": (S, [P, P]),
+    "axr_draw_density_class": (C.c_int32, [P]),
     "axr_graph_begin": (S, [P]),
     "axr_graph_end": (S, [P, PP]),
     "axr_graph_launch": (S, [P, P]),

@@ -9,6 +9,8 @@ Names and argument meaning follow the reference classes:
   BlinnPhongShader, GouraudShader          this library's own shaders
   TiledPipeline   include/tiled_pipeline.hpp (setShader/setCamera/setFramebuffer/drawMesh)
   Renderer.drawMesh                        src/renderer.cpp:16-19
+  Draw, Batch, draw_batch, autotune        the batched form (no reference counterpart)
+  Graph                                    CUDA-graph capture and replay of a context's work
 Every call runs the CUDA library; there is no CPU path.
 """
 from __future__ import annotations
@@ -20,7 +22,8 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import AxrError, CameraDesc, DrawDesc, DrawStats, GroupDesc, MaterialDesc, MeshDesc, ShaderDesc, check
+from ._lib import (AXR_DRAW_CLEAR_COLOR, AXR_DRAW_CLEAR_DEPTH, AXR_TUNE_CLASSES, AxrError, BatchInfo, CameraDesc,
+                   DrawDesc, DrawStats, GroupDesc, MaterialDesc, MeshDesc, ShaderDesc, check)
 
 FLAT, PHONG, PBR, BLINN_PHONG, GOURAUD = 0, 1, 2, 3, 4
 
@@ -70,7 +73,21 @@ class Context:
         check(self.lib.axr_profile_read(self.handle, C.byref(pr)), self.handle)
         return {"draws": pr.draws, "vertex_ms": pr.vertex_ms, "geometry_ms": pr.geometry_ms,
                 "large_ms": pr.large_ms, "scan_ms": pr.scan_ms, "shade_ms": pr.shade_ms,
-                "clipped_ms": pr.clipped_ms, "kernel_launches": pr.kernel_launches}
+                "clipped_ms": pr.clipped_ms, "kernel_launches": pr.kernel_launches,
+                "batch_launches": pr.batch_launches, "batch_vertex_ms": pr.batch_vertex_ms,
+                "batch_face_ms": pr.batch_face_ms, "batch_large_ms": pr.batch_large_ms,
+                "batch_tile_ms": pr.batch_tile_ms}
+
+    def tuning(self) -> list:
+        """The batched form's tuning table: per density class, the largest triangle pixel
+        box rasterised by one thread."""
+        out = (C.c_int32 * AXR_TUNE_CLASSES)()
+        check(self.lib.axr_batch_get_tuning(self.handle, out), self.handle)
+        return list(out)
+
+    def set_tuning(self, small_max_pixels: Sequence[int]) -> None:
+        arr = (C.c_int32 * AXR_TUNE_CLASSES)(*[int(v) for v in small_max_pixels])
+        check(self.lib.axr_batch_set_tuning(self.handle, arr), self.handle)
 
     def close(self) -> None:
         if getattr(self, "handle", None):
@@ -406,4 +423,141 @@ def render_scene(ctx: Context, scene, framebuffer: Optional[Framebuffer] = None,
     pipe.drawMesh(scene.model, m)
     out = fb.read()
     ctx.sync()
+    return out
+
+
+# ---------------------------------------------------------------- batched form
+@dataclasses.dataclass
+class Draw:
+    """One draw of a batch (axr_draw_desc): its own mesh, framebuffer, camera and shader.
+    clear_color (r, g, b, a) / clear_depth: Framebuffer::clearColor / clearDepth before the
+    draw, fused into the batch's tile pass."""
+    mesh: "Mesh"
+    framebuffer: "Framebuffer"
+    camera: "Camera"
+    shader: Shader
+    model: Optional[np.ndarray] = None
+    clear_color: Optional[tuple] = None
+    clear_depth: Optional[float] = None
+
+    def desc(self) -> DrawDesc:
+        d = DrawDesc()
+        d.mesh = self.mesh.handle
+        d.framebuffer = self.framebuffer.handle
+        d.model = (C.c_float * 16)(*_model(self.model))
+        d.camera = self.camera.desc()
+        d.shader = self.shader.desc()
+        flags = 0
+        if self.clear_color is not None:
+            flags |= AXR_DRAW_CLEAR_COLOR
+            d.clear_rgba = (C.c_uint8 * 4)(*[int(v) for v in self.clear_color])
+        if self.clear_depth is not None:
+            flags |= AXR_DRAW_CLEAR_DEPTH
+            d.clear_depth = float(self.clear_depth)
+        d.clear_flags = flags
+        return d
+
+
+def _draw_descs(draws: Sequence[Draw]):
+    arr = (DrawDesc * max(1, len(draws)))()
+    for i, d in enumerate(draws):
+        arr[i] = d.desc()
+    return arr
+
+
+class Batch:
+    """A planned batch (axr_batch): launch() enqueues it; the launch can be captured in a Graph."""
+
+    def __init__(self, ctx: Context, draws: Sequence[Draw]):
+        self.ctx = ctx
+        self.draws = list(draws)
+        h = C.c_void_p()
+        check(ctx.lib.axr_batch_create(ctx.handle, _draw_descs(self.draws), len(self.draws), C.byref(h)), ctx.handle)
+        self.handle = h
+
+    def launch(self) -> None:
+        check(self.ctx.lib.axr_batch_launch(self.ctx.handle, self.handle), self.ctx.handle)
+
+    def info(self) -> dict:
+        i = BatchInfo()
+        check(self.ctx.lib.axr_batch_get_info(self.handle, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in BatchInfo._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.axr_batch_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def draw_batch(ctx: Context, draws: Sequence[Draw]) -> None:
+    """One-shot batch (axr_draw_batch)."""
+    check(ctx.lib.axr_draw_batch(ctx.handle, _draw_descs(draws), len(draws)), ctx.handle)
+
+
+def autotune(ctx: Context, draws: Sequence[Draw], repeats: int = 3) -> list:
+    """Tune the context's per-class raster parameter on these draws; returns the table."""
+    out = (C.c_int32 * AXR_TUNE_CLASSES)()
+    check(ctx.lib.axr_batch_autotune(ctx.handle, _draw_descs(draws), len(draws), int(repeats), out), ctx.handle)
+    return list(out)
+
+
+def density_class(draw: Draw) -> int:
+    d = draw.desc()
+    return int(_lib.load().axr_draw_density_class(C.byref(d)))
+
+
+class Graph:
+    """CUDA graph of the work a context enqueued between begin() and end()."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.handle = None
+
+    def begin(self) -> "Graph":
+        check(self.ctx.lib.axr_graph_begin(self.ctx.handle), self.ctx.handle)
+        return self
+
+    def end(self) -> "Graph":
+        h = C.c_void_p()
+        check(self.ctx.lib.axr_graph_end(self.ctx.handle, C.byref(h)), self.ctx.handle)
+        self.handle = h
+        return self
+
+    def launch(self) -> None:
+        check(self.ctx.lib.axr_graph_launch(self.ctx.handle, self.handle), self.ctx.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.axr_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_draws(ctx: Context, scenes, textures: Optional[dict] = None, meshes: Optional[dict] = None,
+                framebuffers: Optional[list] = None, clear: bool = True) -> list:
+    """Draws for workloads.Scene objects (one framebuffer each; meshes shared by identity of
+    the scene's mesh object, textures by identity of the image)."""
+    textures = {} if textures is None else textures
+    meshes = {} if meshes is None else meshes
+    out = []
+    for k, sc in enumerate(scenes):
+        if id(sc.mesh) not in meshes:
+            meshes[id(sc.mesh)] = Mesh.from_workload(ctx, sc.mesh, textures)
+        fb = framebuffers[k] if framebuffers is not None else Framebuffer(ctx, sc.width, sc.height)
+        b, g, r, a = sc.clear_bgra
+        sh = sc.shader
+        out.append(Draw(meshes[id(sc.mesh)], fb, Camera.from_workload(sc.camera),
+                        Shader(sh.kind, tuple(sh.light_direction), tuple(sh.light_color)), sc.model,
+                        (r, g, b, a) if clear else None, float("inf") if clear else None))
     return out

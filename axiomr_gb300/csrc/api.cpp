@@ -20,8 +20,9 @@
 using namespace axr;
 
 #include "api_types.h"
+#include "api_internal.h"
 
-namespace {
+namespace axr_internal {
 
 thread_local std::string g_no_ctx_error;
 
@@ -46,34 +47,15 @@ axr_status cuda_fail(axr_context* ctx, cudaError_t e, const char* what) {
     return fail(ctx, AXR_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define AXR_CUDA(ctx, call)                                           \
-    do {                                                              \
-        cudaError_t e_ = (call);                                      \
-        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);    \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-    }
-};
-
-template <class T>
-cudaError_t dmalloc(T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) return cudaSuccess;
-    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
-}
-
 void dfree(void* p) {
     if (p) cudaFree(p);
 }
+
+}  // namespace axr_internal
+
+using namespace axr_internal;
+
+namespace {
 
 DevTexture dev_texture(const axr_texture* t) {
     DevTexture d{};
@@ -232,6 +214,8 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, sizeof(DevCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->batch_prof, sizeof(BatchProfile));
+    if (e == cudaSuccess) e = cudaMemset(ctx->batch_prof, 0, sizeof(BatchProfile));
     if (e != cudaSuccess) {
         axr_status st = cuda_fail(nullptr, e, "context setup");
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -239,6 +223,7 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
         if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
         if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
         dfree(ctx->counters);
+        dfree(ctx->batch_prof);
         delete ctx;
         return st;
     }
@@ -255,7 +240,12 @@ void axr_context_destroy(axr_context* ctx) {
     DeviceGuard g(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
+    if (ctx->oneshot) {
+        free_batch(ctx->oneshot);
+        delete ctx->oneshot;
+    }
     dfree(ctx->counters);
+    dfree(ctx->batch_prof);
     free_scratch(ctx);
     if (ctx->aux.stream) cudaStreamSynchronize(ctx->aux.stream);
     if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
@@ -285,6 +275,8 @@ axr_status axr_sync(axr_context* ctx) {
     AXR_CUDA(ctx, cudaMemcpy(&err, &ctx->counters->error, sizeof(err), cudaMemcpyDeviceToHost));
     if (err) {
         AXR_CUDA(ctx, cudaMemset(&ctx->counters->error, 0, sizeof(uint32_t)));
+        if (err & kErrBarrier)
+            return fail(ctx, AXR_E_TIMEOUT, "a grid barrier of the batched kernel timed out (error bits 0x%x)", err);
         return fail(ctx, AXR_E_CAPACITY, "device reported error bits 0x%x", err);
     }
     return AXR_OK;
@@ -390,6 +382,7 @@ axr_status axr_mesh_create(axr_context* ctx, const axr_mesh_desc* d, axr_mesh** 
         base += d->groups[k].face_count;
     }
     m->num_drawn = base;
+    mesh_bounds(d->positions, V, m->bound_center, &m->bound_radius);
     std::vector<DevMaterial> mats(std::max<uint32_t>(1, d->num_materials));
     for (uint32_t k = 0; k < d->num_materials; ++k) {
         const axr_material_desc& md = d->materials[k];
@@ -431,6 +424,7 @@ axr_status axr_mesh_update(axr_context* ctx, axr_mesh* m, const axr_mesh_desc* d
     if (d->num_faces && !d->indices) return fail(ctx, AXR_E_INVALID, "mesh update needs indices");
     std::lock_guard<std::mutex> lk(ctx->mu);
     DeviceGuard g(ctx->device);
+    mesh_bounds(d->positions, d->num_vertices, m->bound_center, &m->bound_radius);
     return upload_mesh_arrays(ctx, m, d);
 }
 
@@ -470,6 +464,7 @@ axr_status axr_framebuffer_create(axr_context* ctx, int32_t width, int32_t heigh
         delete fb;
         return cuda_fail(ctx, e, "framebuffer allocation");
     }
+    encode_framebuffer_maps(fb);
     *out = fb;
     return AXR_OK;
 }
@@ -608,12 +603,6 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
     return AXR_OK;
 }
 
-axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count) {
-    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
-    if (count < 0 || (count > 0 && !draws)) return fail(ctx, AXR_E_INVALID, "bad draw list");
-    return fail(ctx, AXR_E_UNSUPPORTED, "batched draws are not available in this build");
-}
-
 // ---------------------------------------------------------------- graphs
 axr_status axr_graph_begin(axr_context* ctx) {
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
@@ -727,6 +716,14 @@ axr_status axr_profile_read(axr_context* ctx, axr_profile* out) {
         ++r.draws;
     }
     ctx->events_used = 0;
+    BatchProfile bp{};
+    AXR_CUDA(ctx, cudaMemcpy(&bp, ctx->batch_prof, sizeof(bp), cudaMemcpyDeviceToHost));
+    AXR_CUDA(ctx, cudaMemset(ctx->batch_prof, 0, sizeof(bp.phase_ns) + sizeof(bp.launches)));
+    r.batch_launches = bp.launches;
+    r.batch_vertex_ms = bp.phase_ns[0] * 1e-6;
+    r.batch_face_ms = bp.phase_ns[1] * 1e-6;
+    r.batch_large_ms = bp.phase_ns[2] * 1e-6;
+    r.batch_tile_ms = bp.phase_ns[3] * 1e-6;
     r.kernel_launches = ctx->launches;
     *out = r;
     return AXR_OK;

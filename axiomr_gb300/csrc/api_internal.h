@@ -1,0 +1,50 @@
+// Helpers shared by the files that implement C ABI entry points (api.cpp, batch_api.cpp):
+// error reporting into the context, device selection and allocation wrappers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "api_types.h"
+
+namespace axr_internal {
+
+// Record a formatted message as the context's last error (or the thread's, without a
+// context) and return `st`.
+axr_status fail(axr_context* ctx, axr_status st, const char* fmt, ...);
+// AXR_E_OOM for an allocation failure, AXR_E_CUDA otherwise.
+axr_status cuda_fail(axr_context* ctx, cudaError_t e, const char* what);
+void dfree(void* p);
+// Fill fb->color_map / depth_map for TMA tile stores (sets fb->tma; false when the row
+// pitch is not a multiple of 16 bytes or the driver lacks the entry point).
+void encode_framebuffer_maps(axr_framebuffer* fb);
+// Bounding sphere (box centre, largest distance) of n float3 positions.
+void mesh_bounds(const float* pos, uint32_t n, float center[3], float* radius);
+// Release a batch's device memory (the caller synchronises first).
+void free_batch(axr_batch* b);
+
+template <class T>
+cudaError_t dmalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+// Makes `dev` current for the scope and restores the previous device.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace axr_internal
+
+#define AXR_CUDA(ctx, call)                                                      \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) return axr_internal::cuda_fail((ctx), e_, #call); \
+    } while (0)

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "axr.h"
+#include "batch_types.h"
 #include "device_types.h"
 #include "hostmath.h"
 #include "kernels.h"
@@ -38,6 +39,8 @@ struct axr_mesh {
     float* staging = nullptr;  // packed float3 upload area for updates
     uint32_t num_vertices = 0, num_faces = 0, num_groups = 0, num_materials = 0, num_drawn = 0;
     int device = 0;
+    float bound_center[3] = {0.f, 0.f, 0.f};  // bounding sphere of the positions (batch planning)
+    float bound_radius = 0.f;
 };
 
 struct axr_framebuffer {
@@ -47,6 +50,25 @@ struct axr_framebuffer {
     uint32_t* tile_flag = nullptr;
     int32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
     int device = 0;
+    // TMA descriptors of the colour and depth planes (16x16 boxes), valid when tma is set
+    // (the row pitch must be a multiple of 16 bytes: width % 4 == 0)
+    axr::TensorMap128 color_map{}, depth_map{};
+    bool tma = false;
+};
+
+// A planned batch (batch_api.cpp): the draw table and scratch in one device allocation,
+// and one launch description per shader kind present.
+struct axr_batch {
+    struct Launch {
+        int shader;
+        axr::BatchParams params;
+    };
+    int device = 0;
+    void* dev = nullptr;
+    size_t bytes = 0;
+    std::vector<Launch> launches;
+    uint32_t count = 0;
+    uint64_t vertices = 0, faces = 0, pixels = 0, tiles = 0;
 };
 
 struct axr_graph {
@@ -79,6 +101,11 @@ struct axr_context {
     uint32_t large_cap = 0, item_cap = 0, vcap = 0, px_cap = 0;
     int collect_stats = 0;
     int small_max_pixels = 64;
+    // batched form: per density class, the largest pixel box rasterised per thread
+    // (autotuned), and the reusable plan of axr_draw_batch
+    int32_t tune_small[AXR_TUNE_CLASSES] = {64, 64, 64, 64, 64, 64};
+    axr_batch* oneshot = nullptr;
+    axr::BatchProfile* batch_prof = nullptr;  // device-side phase timing of batched launches
     // profiling: per-draw stage events (4 per draw), reused across reads
     bool profile = false;
     std::vector<cudaEvent_t> event_pool;

@@ -1,0 +1,441 @@
+// C ABI of the batched form (include/axr.h, "batched form"): planning a batch of draws into
+// one device allocation, launching it, draw density classes and the autotuner.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <unordered_set>
+#include <vector>
+
+#include "api_internal.h"
+#include "api_types.h"
+#include "batch.h"
+
+using namespace axr;
+using namespace axr_internal;
+
+static_assert(sizeof(CUtensorMap) == sizeof(TensorMap128), "tensor map size");
+static_assert(alignof(TensorMap128) >= 64, "tensor maps are 64-byte aligned");
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// Density class of a draw: estimated mean screen area (pixels) of its front-facing
+// triangles. The mesh's bounding sphere goes through the model matrix (radius scaled by the
+// largest column norm) and the view-projection; its projected ellipse (semi-axes r * |row
+// k of viewProj| / w * size / 2) clamped to the framebuffer, over half the faces.
+int density_class(const axr_draw_desc& d) {
+    const axr_mesh* m = d.mesh;
+    const axr_framebuffer* fb = d.framebuffer;
+    if (!m || !fb || m->num_drawn == 0) return 0;
+    const float* M = d.model;
+    const float* c = m->bound_center;
+    double wc[3];
+    for (int i = 0; i < 3; ++i) wc[i] = (double)M[i] * c[0] + (double)M[4 + i] * c[1] + (double)M[8 + i] * c[2] + M[12 + i];
+    double scale = 0.0;
+    for (int col = 0; col < 3; ++col)
+        scale = std::max(scale, std::sqrt((double)M[4 * col] * M[4 * col] + (double)M[4 * col + 1] * M[4 * col + 1] +
+                                          (double)M[4 * col + 2] * M[4 * col + 2]));
+    const double r = (double)m->bound_radius * scale;
+    const float* V = d.camera.view_proj;
+    auto row = [&](int k) { return (double)V[k] * wc[0] + (double)V[4 + k] * wc[1] + (double)V[8 + k] * wc[2] + V[12 + k]; };
+    auto row_norm = [&](int k) {
+        return std::sqrt((double)V[k] * V[k] + (double)V[4 + k] * V[4 + k] + (double)V[8 + k] * V[8 + k]);
+    };
+    const double w = row(3);
+    if (!(w > r)) return AXR_TUNE_CLASSES - 1;  // the camera is inside or at the sphere
+    const double sx = r * row_norm(0) / w * 0.5 * fb->width;
+    const double sy = r * row_norm(1) / w * 0.5 * fb->height;
+    const double area = std::min(3.14159265358979 * sx * sy, (double)fb->width * (double)fb->height);
+    const double per_tri = area / std::max(1.0, 0.5 * (double)m->num_drawn);
+    int k = 0;
+    for (double lim = 2.0; k < AXR_TUNE_CLASSES - 1 && per_tri >= lim; lim *= 4.0) ++k;
+    return k;
+}
+
+axr_status check_draws(axr_context* ctx, const axr_draw_desc* draws, int32_t count) {
+    if (count < 0 || (count > 0 && !draws)) return fail(ctx, AXR_E_INVALID, "bad draw list");
+    std::unordered_set<const axr_framebuffer*> seen;
+    seen.reserve((size_t)count * 2);
+    for (int32_t i = 0; i < count; ++i) {
+        const axr_draw_desc& d = draws[i];
+        if (!d.mesh || !d.framebuffer) return fail(ctx, AXR_E_INVALID, "draw %d has no mesh or framebuffer", i);
+        if (d.shader.kind < AXR_SHADER_FLAT || d.shader.kind > AXR_SHADER_GOURAUD)
+            return fail(ctx, AXR_E_INVALID, "draw %d: unknown shader kind %d", i, d.shader.kind);
+        if (d.mesh->device != ctx->device || d.framebuffer->device != ctx->device)
+            return fail(ctx, AXR_E_INVALID, "draw %d uses resources of another device", i);
+        if (!seen.insert(d.framebuffer).second)
+            return fail(ctx, AXR_E_INVALID, "draw %d: the framebuffers of a batch must be distinct", i);
+    }
+    return AXR_OK;
+}
+
+uint32_t ceil_div(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
+
+// Build the batch's draw table and launch descriptions into `b`, (re)allocating its device
+// memory when it is too small. `async`: upload with cudaMemcpyAsync on the context stream
+// (the host table is copied before the call returns); otherwise synchronously.
+axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch* b, bool async) {
+    axr_status st = check_draws(ctx, draws, count);
+    if (st != AXR_OK) return st;
+    // draws grouped by shader kind (one launch each), batch order inside a group
+    std::vector<int32_t> order((size_t)count);
+    for (int32_t i = 0; i < count; ++i) order[(size_t)i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t x, int32_t y) { return draws[x].shader.kind < draws[y].shader.kind; });
+    std::vector<std::pair<int, std::pair<size_t, size_t>>> groups;  // kind, [first, last)
+    for (size_t i = 0; i < order.size(); ++i) {
+        const int kind = draws[order[i]].shader.kind;
+        if (groups.empty() || groups.back().first != kind) groups.push_back({kind, {i, i}});
+        groups.back().second.second = i + 1;
+    }
+    // sizes
+    uint64_t faces = 0, verts = 0, pixels = 0, tiles = 0;
+    size_t cache_bytes = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const axr_draw_desc& d = draws[i];
+        faces += d.mesh->num_drawn;
+        verts += d.mesh->num_vertices;
+        pixels += (uint64_t)d.framebuffer->width * d.framebuffer->height;
+        tiles += (uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y;
+        const size_t V = d.mesh->num_vertices;
+        cache_bytes += align256(16 * V) + align256(16 * V * (size_t)vattr_float4s(d.shader.kind));
+    }
+    // shared large-triangle lists: a triangle that finds them full is rasterised by its own
+    // thread instead, so the sizes trade memory for speed only
+    const uint32_t large_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(faces, 65536), 1u << 22);
+    const uint32_t item_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(4 * faces, 1u << 20), 1u << 24);
+    // work units of every draw (the same counts as the loop below assigns)
+    size_t total_units = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const axr_draw_desc& d = draws[i];
+        const bool drawn = d.mesh->num_drawn > 0;
+        total_units += (drawn ? ceil_div(d.mesh->num_vertices, kVertUnit) : 0u) + ceil_div(d.mesh->num_drawn, kFaceUnit);
+        if (drawn || (d.clear_flags & (AXR_DRAW_CLEAR_COLOR | AXR_DRAW_CLEAR_DEPTH)))
+            total_units += ceil_div((uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y, kTileUnit);
+    }
+    const size_t table_bytes = align256(sizeof(BatchDraw) * (size_t)std::max(count, 1));
+    const size_t units_bytes = align256(sizeof(UnitRef) * std::max<size_t>(total_units, 1));
+    const size_t list_bytes = align256(sizeof(LargeTri) * (size_t)large_cap) +
+                              align256(sizeof(uint32_t) * (size_t)large_cap) +
+                              align256(sizeof(LargeItem) * (size_t)item_cap);
+    const size_t need = table_bytes + units_bytes + align256(cache_bytes) + list_bytes;
+    if (need > b->bytes) {
+        if (ctx->capturing) return fail(ctx, AXR_E_CAPACITY, "a batch cannot be planned during graph capture");
+        AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        free_batch(b);
+        AXR_CUDA(ctx, cudaMalloc(&b->dev, need));
+        b->bytes = need;
+    }
+    unsigned char* base = static_cast<unsigned char*>(b->dev);
+    BatchDraw* d_table = reinterpret_cast<BatchDraw*>(base);
+    UnitRef* d_units = reinterpret_cast<UnitRef*>(base + table_bytes);
+    unsigned char* cache = base + table_bytes + units_bytes;
+    unsigned char* lists = cache + align256(cache_bytes);
+    LargeTri* d_large = reinterpret_cast<LargeTri*>(lists);
+    uint32_t* d_large_draw = reinterpret_cast<uint32_t*>(lists + align256(sizeof(LargeTri) * (size_t)large_cap));
+    LargeItem* d_items = reinterpret_cast<LargeItem*>(reinterpret_cast<unsigned char*>(d_large_draw) +
+                                                      align256(sizeof(uint32_t) * (size_t)large_cap));
+
+    std::vector<BatchDraw> table((size_t)std::max(count, 1));
+    std::vector<UnitRef> units;
+    units.reserve(total_units);
+    b->launches.clear();
+    for (const auto& g : groups) {
+        const size_t first = g.second.first, last = g.second.second, n = last - first;
+        std::vector<UnitRef> uv, uf, ut;
+        for (size_t k = 0; k < n; ++k) {
+            const axr_draw_desc& d = draws[order[first + k]];
+            const axr_mesh* m = d.mesh;
+            const axr_framebuffer* fb = d.framebuffer;
+            BatchDraw& bd = table[first + k];
+            std::memset(&bd, 0, sizeof(bd));
+            bd.color_map = fb->color_map;
+            bd.depth_map = fb->depth_map;
+            DrawParams& p = bd.p;
+            p.mesh = DevMesh{m->pos, m->nrm, m->tan, m->bit, m->uv, m->idx, m->groups, m->materials,
+                             m->num_vertices, m->num_faces, m->num_groups, m->num_drawn};
+            p.target = DevTarget{fb->color, fb->depth, fb->key, fb->tile_flag,
+                                 fb->width, fb->height, fb->tiles_x, fb->tiles_y};
+            p.u = make_uniforms(d.camera, d.shader, d.model);
+            float4* vscreen = reinterpret_cast<float4*>(cache);
+            cache += align256(16 * (size_t)m->num_vertices);
+            float4* vattr = reinterpret_cast<float4*>(cache);
+            cache += align256(16 * (size_t)m->num_vertices * (size_t)vattr_float4s(d.shader.kind));
+            p.scratch = DevScratch{ctx->counters, d_large, d_items, vscreen, vattr, nullptr, nullptr,
+                                   large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw};
+            p.small_max_pixels = ctx->tune_small[density_class(d)];
+            p.draw = (uint32_t)k;
+            bd.flags = (d.clear_flags & AXR_DRAW_CLEAR_COLOR ? kBatchClearColor : 0u) |
+                       (d.clear_flags & AXR_DRAW_CLEAR_DEPTH ? kBatchClearDepth : 0u) | (fb->tma ? kBatchTma : 0u);
+            // bytes B, G, R, A (src/framebuffer.cpp:26-36)
+            bd.clear_bgra = ((uint32_t)d.clear_rgba[3] << 24) | ((uint32_t)d.clear_rgba[0] << 16) |
+                            ((uint32_t)d.clear_rgba[1] << 8) | (uint32_t)d.clear_rgba[2];
+            bd.clear_depth = d.clear_depth;
+            const bool drawn = m->num_drawn > 0;
+            const uint32_t nv = drawn ? ceil_div(m->num_vertices, kVertUnit) : 0u;
+            const uint32_t nf = ceil_div(m->num_drawn, kFaceUnit);
+            const uint32_t nt = (drawn || bd.flags & (kBatchClearColor | kBatchClearDepth))
+                                    ? ceil_div((uint64_t)fb->tiles_x * fb->tiles_y, kTileUnit)
+                                    : 0u;
+            for (uint32_t j = 0; j < nv; ++j) uv.push_back(UnitRef{(uint32_t)k, j});
+            for (uint32_t j = 0; j < nf; ++j) uf.push_back(UnitRef{(uint32_t)k, j});
+            for (uint32_t j = 0; j < nt; ++j) ut.push_back(UnitRef{(uint32_t)k, j});
+        }
+        const size_t unit_at = units.size();
+        units.insert(units.end(), uv.begin(), uv.end());
+        units.insert(units.end(), uf.begin(), uf.end());
+        units.insert(units.end(), ut.begin(), ut.end());
+        axr_batch::Launch L{};
+        L.shader = g.first;
+        BatchParams& bp = L.params;
+        bp.draws = d_table + first;
+        bp.units = d_units + unit_at;
+        bp.counters = ctx->counters;
+        bp.large = d_large;
+        bp.items = d_items;
+        bp.large_draw = d_large_draw;
+        bp.count = (uint32_t)n;
+        bp.vert_units = (uint32_t)uv.size();
+        bp.face_units = (uint32_t)uf.size();
+        bp.tile_units = (uint32_t)ut.size();
+        bp.large_cap = large_cap;
+        bp.item_cap = item_cap;
+        if (bp.vert_units + bp.face_units + bp.tile_units > 0) b->launches.push_back(L);
+    }
+    if (async) {
+        AXR_CUDA(ctx, cudaMemcpyAsync(d_table, table.data(), sizeof(BatchDraw) * table.size(), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        if (!units.empty())
+            AXR_CUDA(ctx, cudaMemcpyAsync(d_units, units.data(), sizeof(UnitRef) * units.size(), cudaMemcpyHostToDevice,
+                                          ctx->stream));
+    } else {
+        AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        AXR_CUDA(ctx, cudaMemcpy(d_table, table.data(), sizeof(BatchDraw) * table.size(), cudaMemcpyHostToDevice));
+        if (!units.empty())
+            AXR_CUDA(ctx, cudaMemcpy(d_units, units.data(), sizeof(UnitRef) * units.size(), cudaMemcpyHostToDevice));
+    }
+    b->device = ctx->device;
+    b->count = (uint32_t)count;
+    b->vertices = verts;
+    b->faces = faces;
+    b->pixels = pixels;
+    b->tiles = tiles;
+    return AXR_OK;
+}
+
+axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
+    for (const axr_batch::Launch& L : b->launches) {
+        BatchParams bp = L.params;
+        bp.collect_stats = ctx->collect_stats;
+        bp.prof = ctx->profile ? ctx->batch_prof : nullptr;
+        AXR_CUDA(ctx, launch_batch(L.shader, bp, ctx->cfg.num_sms, ctx->stream, &ctx->launches));
+    }
+    return AXR_OK;
+}
+
+}  // namespace
+
+namespace axr_internal {
+
+void encode_framebuffer_maps(axr_framebuffer* fb) {
+    fb->tma = false;
+    if (fb->width % 4 != 0) return;  // the row pitch of a tensor map is a multiple of 16 bytes
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return;
+    const cuuint64_t dims[2] = {(cuuint64_t)fb->width, (cuuint64_t)fb->height};
+    const cuuint64_t pitch[1] = {(cuuint64_t)fb->width * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kTile, (cuuint32_t)kTile};
+    const cuuint32_t step[2] = {1, 1};
+    const CUresult rc = encode(reinterpret_cast<CUtensorMap*>(&fb->color_map), CU_TENSOR_MAP_DATA_TYPE_UINT32, 2,
+                               fb->color, dims, pitch, box, step, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult rd = encode(reinterpret_cast<CUtensorMap*>(&fb->depth_map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                               fb->depth, dims, pitch, box, step, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    fb->tma = rc == CUDA_SUCCESS && rd == CUDA_SUCCESS;
+}
+
+void mesh_bounds(const float* pos, uint32_t n, float center[3], float* radius) {
+    center[0] = center[1] = center[2] = 0.f;
+    *radius = 0.f;
+    if (!pos || n == 0) return;
+    float lo[3] = {pos[0], pos[1], pos[2]}, hi[3] = {pos[0], pos[1], pos[2]};
+    for (uint32_t i = 1; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], pos[3ull * i + k]);
+            hi[k] = std::max(hi[k], pos[3ull * i + k]);
+        }
+    for (int k = 0; k < 3; ++k) center[k] = 0.5f * (lo[k] + hi[k]);
+    double r2 = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const double t = (double)pos[3ull * i + k] - center[k];
+            s += t * t;
+        }
+        r2 = std::max(r2, s);
+    }
+    *radius = (float)std::sqrt(r2) * 1.0001f;
+}
+
+void free_batch(axr_batch* b) {
+    if (!b) return;
+    dfree(b->dev);
+    b->dev = nullptr;
+    b->bytes = 0;
+    b->launches.clear();
+}
+
+}  // namespace axr_internal
+
+extern "C" {
+
+axr_status axr_batch_create(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch** out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    auto* b = new axr_batch();
+    axr_status st = plan_batch(ctx, draws, count, b, false);
+    if (st != AXR_OK) {
+        free_batch(b);
+        delete b;
+        return st;
+    }
+    *out = b;
+    return AXR_OK;
+}
+
+axr_status axr_batch_launch(axr_context* ctx, axr_batch* b) {
+    if (!ctx || !b) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    if (b->device != ctx->device) return fail(ctx, AXR_E_INVALID, "batch planned for another device");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    return launch_planned(ctx, b);
+}
+
+void axr_batch_destroy(axr_context* ctx, axr_batch* b) {
+    if (!b) return;
+    DeviceGuard g(b->device);
+    if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_batch(b);
+    delete b;
+}
+
+axr_status axr_batch_get_info(const axr_batch* b, axr_batch_info* out) {
+    if (!b || !out) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    out->draws = b->count;
+    out->launches = (uint32_t)b->launches.size();
+    out->vertices = b->vertices;
+    out->faces = b->faces;
+    out->pixels = b->pixels;
+    out->tiles = b->tiles;
+    out->device_bytes = b->bytes;
+    return AXR_OK;
+}
+
+axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->capturing) return fail(ctx, AXR_E_INVALID, "axr_draw_batch cannot be captured; capture axr_batch_launch");
+    DeviceGuard g(ctx->device);
+    if (!ctx->oneshot) ctx->oneshot = new axr_batch();
+    axr_status st = plan_batch(ctx, draws, count, ctx->oneshot, true);
+    if (st != AXR_OK) return st;
+    return launch_planned(ctx, ctx->oneshot);
+}
+
+int32_t axr_draw_density_class(const axr_draw_desc* draw) { return draw ? density_class(*draw) : 0; }
+
+axr_status axr_batch_get_tuning(const axr_context* ctx, int32_t small_max_pixels[AXR_TUNE_CLASSES]) {
+    if (!ctx || !small_max_pixels) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    std::memcpy(small_max_pixels, ctx->tune_small, sizeof(ctx->tune_small));
+    return AXR_OK;
+}
+
+axr_status axr_batch_set_tuning(axr_context* ctx, const int32_t small_max_pixels[AXR_TUNE_CLASSES]) {
+    if (!ctx || !small_max_pixels) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    for (int k = 0; k < AXR_TUNE_CLASSES; ++k)
+        if (small_max_pixels[k] < 0 || small_max_pixels[k] > 65536)
+            return fail(ctx, AXR_E_INVALID, "class %d: pixel box limit %d (0..65536)", k, small_max_pixels[k]);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::memcpy(ctx->tune_small, small_max_pixels, sizeof(ctx->tune_small));
+    return AXR_OK;
+}
+
+axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int32_t count, int32_t repeats,
+                              int32_t out_small_max_pixels[AXR_TUNE_CLASSES]) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    if (repeats < 1) repeats = 1;
+    axr_status st = check_draws(ctx, draws, count);
+    if (st != AXR_OK) return st;
+    static const int32_t kCandidates[] = {16, 32, 64, 128, 256};
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->capturing) return fail(ctx, AXR_E_INVALID, "cannot tune during graph capture");
+    DeviceGuard g(ctx->device);
+    std::vector<std::vector<axr_draw_desc>> by_class(AXR_TUNE_CLASSES);
+    for (int32_t i = 0; i < count; ++i) by_class[(size_t)density_class(draws[i])].push_back(draws[i]);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    AXR_CUDA(ctx, cudaEventCreate(&e0));
+    AXR_CUDA(ctx, cudaEventCreate(&e1));
+    axr_batch trial;
+    st = AXR_OK;
+    for (int k = 0; k < AXR_TUNE_CLASSES && st == AXR_OK; ++k) {
+        const std::vector<axr_draw_desc>& sub = by_class[(size_t)k];
+        if (sub.empty()) continue;
+        float best_ms = 0.f;
+        int32_t best = ctx->tune_small[k];
+        for (int32_t cand : kCandidates) {
+            ctx->tune_small[k] = cand;
+            st = plan_batch(ctx, sub.data(), (int32_t)sub.size(), &trial, false);
+            if (st != AXR_OK) break;
+            if ((st = launch_planned(ctx, &trial)) != AXR_OK) break;  // warm-up
+            cudaError_t e = cudaEventRecord(e0, ctx->stream);
+            for (int32_t r = 0; r < repeats && e == cudaSuccess && st == AXR_OK; ++r) st = launch_planned(ctx, &trial);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) st = cuda_fail(ctx, e, "autotune timing");
+            if (st != AXR_OK) break;
+            if (best_ms == 0.f || ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+        ctx->tune_small[k] = best;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    free_batch(&trial);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != AXR_OK) return st;
+    if (out_small_max_pixels) std::memcpy(out_small_max_pixels, ctx->tune_small, sizeof(ctx->tune_small));
+    return AXR_OK;
+}
+
+}  // extern "C"

@@ -25,6 +25,11 @@ constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;  // no triangle 
 
 enum ShaderKind : int32_t { kFlat = 0, kPhong = 1, kPBR = 2, kBlinnPhong = 3, kGouraud = 4 };
 
+// float4s of cached vertex-shader outputs per vertex for a shader kind.
+constexpr int vattr_float4s(int shader) {
+    return (shader == kPhong || shader == kPBR) ? 4 : (shader == kBlinnPhong ? 2 : 1);
+}
+
 struct DevTexture {
     const uint32_t* texels;
     int32_t width, height;
@@ -100,7 +105,8 @@ struct DevCounters {
     uint32_t item_head;       // next LargeItem to hand out
     uint32_t shade_count;     // covered pixels (unclipped winners) found by the key scan
     uint32_t clip_count;      // covered pixels whose winner is a clipped triangle
-    uint32_t pad_[2];
+    uint32_t bar_count;       // batched kernel: CTAs arrived at the current grid barrier
+    uint32_t bar_gen;         // batched kernel: grid barriers completed
     uint32_t error;           // sticky error bits (kErr*), cleared by axr_sync
     unsigned long long stat_triangles;   // triangles that passed clip + cull
     unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
@@ -109,6 +115,7 @@ struct DevCounters {
 };
 
 constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
+constexpr unsigned kBatchCountersReset = 7 * sizeof(uint32_t);  // + the grid-barrier words
 constexpr uint32_t kErrOrdinal = 1u;  // more faces than a depth key can order
 constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh (face skipped)
 
@@ -132,6 +139,7 @@ struct DevScratch {
     uint32_t px_cap;          // >= pixels of the target (shade and clip_px capacity)
     int32_t collect_stats;
     int32_t pad_;
+    uint32_t* large_draw;     // batched draws: draw index of each LargeTri slot (NULL per draw)
 };
 
 struct DrawParams {
@@ -140,7 +148,7 @@ struct DrawParams {
     DevUniforms u;
     DevScratch scratch;
     int32_t small_max_pixels;  // triangles whose pixel box is at most this are rasterised per thread
-    int32_t pad_;
+    uint32_t draw;             // index of the draw in its batch (0 for a single draw)
 };
 
 }  // namespace axr

@@ -1,0 +1,313 @@
+// Device-side steps of one draw, shared by the per-draw kernels (kernels.cu) and the
+// batched persistent kernel (batch.cu): per-vertex transform and shading, per-face clip /
+// cull / setup / small-triangle raster, the large-triangle tile raster, and the shading of
+// one pixel's winning fragment. The kernels differ only in how work is handed out.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "raster.cuh"
+#include "shade.cuh"
+
+namespace axr {
+namespace {
+
+constexpr uint32_t kNoTile = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
+
+// A tile that holds at least one depth key is flagged for the key scan (a plain store:
+// every writer stores the same value).
+__device__ __forceinline__ void mark_tile(const DevTarget& t, uint32_t tile) { t.tile_flag[tile] = 1u; }
+
+__device__ __forceinline__ uint32_t tile_of(const DevTarget& t, int px, int py) {
+    return (uint32_t)(py >> 4) * (uint32_t)t.tiles_x + (uint32_t)(px >> 4);
+}
+
+// Visibility write of one covered pixel (no return value used: compiles to a reduction).
+// Returns whether a key was written.
+__device__ __forceinline__ bool write_key(const DevTarget& t, int px, int py, float z, uint32_t tag) {
+    if (!(z < __int_as_float(0x7f800000))) return false;  // +inf and NaN never pass early-Z
+    atomicMin(&t.key[(uint32_t)py * (uint32_t)t.width + (uint32_t)px], make_key(z, tag));
+    return true;
+}
+
+struct GeomStats {
+    uint32_t tris, frags, large;
+};
+
+// Rasterise a small triangle's pixel box in this thread; returns whether any key was
+// written. Walks the box the way the reference's tile raster does: per 16-pixel tile
+// column and row, the row start (a*(sx+0.5) + b*(py+0.5)) + c and its 8-pixel step are
+// computed once, then each pixel adds a*lane (eval_pixel gives the same bits per pixel).
+__device__ bool raster_box(const DevTarget& t, const Edges& e, uint32_t tag, GeomStats& st) {
+    bool wrote = false;
+    for (int tx = e.x_lo >> 4; tx <= (e.x_hi - 1) >> 4; ++tx) {
+        const int sx = max(tx * kTile, e.x_lo);
+        const int ex = min((tx + 1) * kTile, e.x_hi);
+        const float fsx = fadd((float)sx, 0.5f);
+        float as[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) as[k] = fmul(e.a[k], fsx);
+        for (int py = e.y_lo; py < e.y_hi; ++py) {
+            const float fpy = fadd((float)py, 0.5f);
+            float r0[3], r8[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                r0[k] = fadd(fadd(as[k], fmul(e.b[k], fpy)), e.c[k]);
+                r8[k] = fadd(r0[k], fmul(e.a[k], 8.0f));
+            }
+            for (int px = sx; px < ex; ++px) {
+                const int i = px - sx;
+                const float lane = (float)(i & 7);
+                float cov[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) cov[k] = fadd(i >= 8 ? r8[k] : r0[k], fmul(e.a[k], lane));
+                if (cov[0] >= 0.f && cov[1] >= 0.f && cov[2] >= 0.f) {
+                    ++st.frags;
+                    const float al = fmul(cov[0], e.inv_area), be = fmul(cov[1], e.inv_area),
+                                ga = fmul(cov[2], e.inv_area);
+                    const float z = fadd(fadd(fmul(e.z[0], al), fmul(e.z[1], be)), fmul(e.z[2], ga));
+                    wrote |= write_key(t, px, py, z, tag);
+                }
+            }
+        }
+    }
+    return wrote;
+}
+
+__device__ __forceinline__ uint32_t tiles_of(const Edges& e, uint32_t& ntx) {
+    int tx0 = e.x_lo >> 4, tx1 = (e.x_hi - 1) >> 4;
+    int ty0 = e.y_lo >> 4, ty1 = (e.y_hi - 1) >> 4;
+    ntx = (uint32_t)(tx1 - tx0 + 1);
+    return ntx * (uint32_t)(ty1 - ty0 + 1);
+}
+
+__device__ void mark_box(const DevTarget& t, const Edges& e) {
+    for (int ty = e.y_lo >> 4; ty <= (e.y_hi - 1) >> 4; ++ty)
+        for (int tx = e.x_lo >> 4; tx <= (e.x_hi - 1) >> 4; ++tx)
+            mark_tile(t, (uint32_t)ty * (uint32_t)t.tiles_x + (uint32_t)tx);
+}
+
+__device__ __forceinline__ void store_large(LargeTri* dst, const Edges& e, uint32_t tag) {
+    float4* d = reinterpret_cast<float4*>(dst);
+    d[0] = make_float4(e.a[0], e.b[0], e.c[0], e.a[1]);
+    d[1] = make_float4(e.b[1], e.c[1], e.a[2], e.b[2]);
+    d[2] = make_float4(e.c[2], e.inv_area, e.z[0], e.z[1]);
+    uint32_t xs = (uint32_t)e.x_lo | ((uint32_t)e.x_hi << 16);
+    uint32_t ys = (uint32_t)e.y_lo | ((uint32_t)e.y_hi << 16);
+    d[3] = make_float4(e.z[2], __uint_as_float(tag), __uint_as_float(xs), __uint_as_float(ys));
+}
+
+__device__ __forceinline__ void load_large(const LargeTri* src, Edges& e, uint32_t& tag) {
+    const float4* s = reinterpret_cast<const float4*>(src);
+    float4 v0 = s[0], v1 = s[1], v2 = s[2], v3 = s[3];
+    e.a[0] = v0.x; e.b[0] = v0.y; e.c[0] = v0.z; e.a[1] = v0.w;
+    e.b[1] = v1.x; e.c[1] = v1.y; e.a[2] = v1.z; e.b[2] = v1.w;
+    e.c[2] = v2.x; e.inv_area = v2.y; e.z[0] = v2.z; e.z[1] = v2.w;
+    e.z[2] = v3.x;
+    tag = __float_as_uint(v3.y);
+    uint32_t xs = __float_as_uint(v3.z), ys = __float_as_uint(v3.w);
+    e.x_lo = (int)(xs & 0xFFFFu); e.x_hi = (int)(xs >> 16);
+    e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
+}
+
+// One triangle that survived clipping: cull, set up, then rasterise it here or queue its
+// tiles. *single_tile receives the one tile a small triangle wrote to (the caller marks
+// it after deduplicating across the warp); boxes spanning several tiles are marked here.
+__device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag, GeomStats& st,
+                              uint32_t* single_tile) {
+    if (is_backface(s)) return;
+    ++st.tris;
+    Edges e;
+    if (!edge_setup(s, p.target.width, p.target.height, e)) return;
+    const int npx = (e.x_hi - e.x_lo) * (e.y_hi - e.y_lo);
+    DevCounters* c = p.scratch.counters;
+    if (npx <= p.small_max_pixels) {
+        if (raster_box(p.target, e, tag, st)) {
+            uint32_t ntx;
+            if (tiles_of(e, ntx) == 1u && *single_tile == kNoTile)
+                *single_tile = tile_of(p.target, e.x_lo, e.y_lo);
+            else
+                mark_box(p.target, e);
+        }
+        return;
+    }
+    uint32_t ntx;
+    const uint32_t nt = tiles_of(e, ntx);
+    const uint32_t slot = atomicAdd(&c->large_count, 1u);
+    const uint32_t base = atomicAdd(&c->item_count, nt);
+    const uint32_t icap = p.scratch.item_cap;
+    if (slot < p.scratch.large_cap && base + nt <= icap && base + nt > base) {
+        store_large(&p.scratch.large[slot], e, tag);
+        if (p.scratch.large_draw) p.scratch.large_draw[slot] = p.draw;
+        for (uint32_t k = 0; k < nt; ++k) p.scratch.items[base + k] = LargeItem{slot, k};
+        ++st.large;
+    } else {
+        // lists full: mark the reserved items empty and rasterise the triangle here
+        for (uint32_t k = base; k < icap && k - base < nt; ++k) p.scratch.items[k] = LargeItem{kNoItem, 0u};
+        if (raster_box(p.target, e, tag, st)) mark_box(p.target, e);
+    }
+}
+
+
+// IShader::vertex of vertex i plus its screen position, NDC depth and clip-plane masks
+// (the per-vertex part of the reference's Triangle ctor, src/tiled_pipeline.cpp:53-72).
+template <int S>
+__device__ __forceinline__ void vertex_one(const DrawParams& p, uint32_t i) {
+    constexpr int A = ShaderAttrs<S>::mask;
+    CVFull v = load_vertex<A>(p.mesh, i);
+    f4 clip = mat4_mul(p.u.mvp, v.pos.x, v.pos.y, v.pos.z, 1.0f);
+    f3 sc = screen_vertex(clip, (float)p.target.width, (float)p.target.height);
+    p.scratch.vscreen[i] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(plane_masks(clip)));
+    pack_vsout<S>(vertex_shader<S>(p.u, v), &p.scratch.vattr[(size_t)VAttr<S>::n * i]);
+}
+
+// Face at draw-order position o (< num_drawn): clip classification, cull, setup and
+// raster or queueing (src/tiled_pipeline.cpp:195-240, 436-487).
+// kCoherent: the vertex cache was written earlier in the same launch (plain loads).
+template <bool kCoherent = false>
+__device__ __forceinline__ void geometry_one(const DrawParams& p, uint32_t o, GeomStats& st, uint32_t& single_tile) {
+    if (o > kMaxOrdinal) {
+        atomicOr(&p.scratch.counters->error, kErrOrdinal);
+        return;
+    }
+    const FaceRef fr = face_of(p.mesh, o);
+    const uint3 f = load_face(p.mesh, fr.face);
+    const uint32_t nv = p.mesh.num_vertices;
+    if (f.x >= nv || f.y >= nv || f.z >= nv) {
+        atomicOr(&p.scratch.counters->error, kErrIndex);
+        return;
+    }
+    const float4* vs = p.scratch.vscreen;
+    const float4 g0 = ld_cached<kCoherent>(&vs[f.x]), g1 = ld_cached<kCoherent>(&vs[f.y]),
+                 g2 = ld_cached<kCoherent>(&vs[f.z]);
+    const int cls = classify_masks(__float_as_uint(g0.w), __float_as_uint(g1.w), __float_as_uint(g2.w));
+    if (cls == 3) {
+        Screen s;
+        s.x[0] = g0.x; s.y[0] = g0.y; s.z[0] = g0.z;
+        s.x[1] = g1.x; s.y[1] = g1.y; s.z[1] = g1.z;
+        s.x[2] = g2.x; s.y[2] = g2.y; s.z[2] = g2.z;
+        screen_bbox(s);
+        emit_triangle(p, s, o << 4, st, &single_tile);
+    } else if (cls < 0) {
+        CVClip a[kMaxClipVerts], b[kMaxClipVerts];
+        a[0].clip = load_clip(p.mesh, p.u.mvp, f.x);
+        a[1].clip = load_clip(p.mesh, p.u.mvp, f.y);
+        a[2].clip = load_clip(p.mesh, p.u.mvp, f.z);
+        CVClip* out;
+        const int n = clip_triangle<0>(a, b, &out);
+        for (int j = 0; 3 * j + 2 < n; ++j) {
+            Screen s;
+            screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width,
+                         p.target.height, s);
+            uint32_t tile = kNoTile;
+            emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile);
+            if (tile != kNoTile) mark_tile(p.target, tile);
+        }
+    }
+}
+
+// Warp-wide end of the geometry step: one mark per distinct single tile in the warp, and
+// the statistics. All 32 lanes must call it.
+__device__ __forceinline__ void geometry_warp_tail(const DevTarget& t, DevCounters* c, bool stats, const GeomStats& st,
+                                                   uint32_t single_tile) {
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, single_tile);
+    if (single_tile != kNoTile && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) mark_tile(t, single_tile);
+    if (stats) {
+        const unsigned full = 0xFFFFFFFFu;
+        uint32_t tr = __reduce_add_sync(full, st.tris), fr = __reduce_add_sync(full, st.frags);
+        uint32_t l = __reduce_add_sync(full, st.large);
+        if ((threadIdx.x & 31) == 0) {
+            if (tr) atomicAdd(&c->stat_triangles, (unsigned long long)tr);
+            if (fr) atomicAdd(&c->stat_fragments, (unsigned long long)fr);
+            if (l) atomicAdd(&c->stat_large, (unsigned long long)l);
+        }
+    }
+}
+
+// One large-triangle work item: the warp evaluates the 256 pixels of tile `item_tile` of
+// the triangle's tile box, 8 per lane, and flags the tile if a key was written.
+__device__ __forceinline__ void large_tile(const DevTarget& t, const Edges& e, uint32_t tag, uint32_t item_tile,
+                                           uint32_t& frags) {
+    const int lane = threadIdx.x & 31;
+    uint32_t ntx;
+    tiles_of(e, ntx);
+    const int tx = (e.x_lo >> 4) + (int)(item_tile % ntx);
+    const int ty = (e.y_lo >> 4) + (int)(item_tile / ntx);
+    const int px = tx * kTile + (lane & 15);
+    bool wrote = false;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int py = ty * kTile + (lane >> 4) + 2 * r;
+        if (px >= e.x_lo && px < e.x_hi && py >= e.y_lo && py < e.y_hi) {
+            PixelEval pe = eval_pixel(e, px, py);
+            if (pe.covered) {
+                ++frags;
+                wrote |= write_key(t, px, py, pe.z, tag);
+            }
+        }
+    }
+    if (__any_sync(0xFFFFFFFFu, wrote) && lane == 0) mark_tile(t, (uint32_t)ty * (uint32_t)t.tiles_x + (uint32_t)tx);
+}
+
+// Winner inputs of an unclipped tag: screen positions from the vertex cache and the
+// cached vertex-shader outputs.
+template <int S, bool kCoherent = false>
+__device__ __forceinline__ uint32_t winner_inputs(const DrawParams& p, uint32_t tag, Screen& s, VSOut* vo) {
+    const FaceRef fr = face_of(p.mesh, tag >> 4);
+    const uint3 f = load_face(p.mesh, fr.face);
+    const uint32_t vi[3] = {f.x, f.y, f.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float4 g = ld_cached<kCoherent>(&p.scratch.vscreen[vi[k]]);
+        s.x[k] = g.x;
+        s.y[k] = g.y;
+        s.z[k] = g.z;
+        vo[k] = unpack_vsout<S, kCoherent>(&p.scratch.vattr[(size_t)VAttr<S>::n * vi[k]]);
+    }
+    screen_bbox(s);
+    return fr.material;
+}
+
+// Winner inputs of a clipped tag: the clipper re-run on the face's raw vertex attributes
+// (the geometry stage's clip, now carrying attributes; src/pipeline.cpp:243-272), output
+// triangle j of the tag. Returns false if the tag names no output triangle.
+template <int S>
+__device__ bool clipped_inputs(const DrawParams& p, uint32_t tag, Screen& s, VSOut* vo, uint32_t& material) {
+    constexpr int A = ShaderAttrs<S>::mask;
+    const FaceRef fr = face_of(p.mesh, tag >> 4);
+    const uint3 f = load_face(p.mesh, fr.face);
+    CVFull a[kMaxClipVerts], b[kMaxClipVerts];
+    a[0] = load_vertex<A>(p.mesh, f.x);
+    a[1] = load_vertex<A>(p.mesh, f.y);
+    a[2] = load_vertex<A>(p.mesh, f.z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) a[k].clip = mat4_mul(p.u.mvp, a[k].pos.x, a[k].pos.y, a[k].pos.z, 1.0f);
+    CVFull* out;
+    const int cnt = clip_triangle<A>(a, b, &out);
+    const int j = (int)(tag & 7u);
+    if (3 * j + 2 >= cnt) return false;  // cannot happen: the tag came from this clip
+    screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width, p.target.height, s);
+    for (int k = 0; k < 3; ++k) vo[k] = vertex_shader<S>(p.u, out[3 * j + k]);
+    material = fr.material;
+    return true;
+}
+
+// Fragment of the winner at (px, py): exact barycentrics and depth, the merge test against
+// `old_depth` (tile depth < framebuffer depth, strict; src/tiled_pipeline.cpp:1171-1174)
+// and the shader. Returns whether the fragment is written.
+template <int S>
+__device__ __forceinline__ bool shade_pixel(const DrawParams& p, int px, int py, uint32_t material, Screen& s,
+                                            const VSOut* vo, float old_depth, uint32_t& bgra, float& z) {
+    Edges e;
+    if (!edge_setup(s, p.target.width, p.target.height, e)) return false;
+    const PixelEval r = eval_pixel(e, px, py);
+    if (!(r.z < old_depth)) return false;
+    const f4 col = fragment_shader<S>(p.u, p.mesh.materials[material], mk3(r.alpha, r.beta, r.gamma), vo);
+    bgra = pack_bgra(col);
+    z = r.z;
+    return true;
+}
+
+}  // namespace
+}  // namespace axr

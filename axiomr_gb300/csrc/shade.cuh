@@ -103,7 +103,7 @@ __device__ __forceinline__ VSOut vertex_shader(const DevUniforms& u, const CVFul
 //   Phong, PBR  [world, uv.x] [t, uv.y] [b, 0] [n, 0]
 template <int S>
 struct VAttr {
-    static constexpr int n = (S == kPhong || S == kPBR) ? 4 : (S == kBlinnPhong ? 2 : 1);
+    static constexpr int n = vattr_float4s(S);
 };
 constexpr int kMaxVAttr = 4;
 
@@ -124,23 +124,31 @@ __device__ __forceinline__ void pack_vsout(const VSOut& o, float4* dst) {
     }
 }
 
-template <int S>
+// Load of cached per-vertex data: through the read-only cache when it was written by an
+// earlier launch, a plain load when it was written earlier in the same (persistent) launch.
+template <bool kCoherent>
+__device__ __forceinline__ float4 ld_cached(const float4* p) {
+    if constexpr (kCoherent) return *p;
+    else return __ldg(p);
+}
+
+template <int S, bool kCoherent = false>
 __device__ __forceinline__ VSOut unpack_vsout(const float4* src) {
     VSOut o;
     if constexpr (S == kFlat) {
-        float4 a = __ldg(&src[0]);
+        float4 a = ld_cached<kCoherent>(&src[0]);
         o.normal = mk3(a.x, a.y, a.z);
     } else if constexpr (S == kGouraud) {
-        float4 a = __ldg(&src[0]);
+        float4 a = ld_cached<kCoherent>(&src[0]);
         o.normal = mk3(a.x, a.y, a.z);
         o.uv = mk2(a.w, 0.0f);
     } else if constexpr (S == kBlinnPhong) {
-        float4 a = __ldg(&src[0]), b = __ldg(&src[1]);
+        float4 a = ld_cached<kCoherent>(&src[0]), b = ld_cached<kCoherent>(&src[1]);
         o.world = mk3(a.x, a.y, a.z);
         o.normal = mk3(b.x, b.y, b.z);
         o.uv = mk2(a.w, b.w);
     } else {
-        float4 a = __ldg(&src[0]), b = __ldg(&src[1]), c = __ldg(&src[2]), d = __ldg(&src[3]);
+        float4 a = ld_cached<kCoherent>(&src[0]), b = ld_cached<kCoherent>(&src[1]), c = ld_cached<kCoherent>(&src[2]), d = ld_cached<kCoherent>(&src[3]);
         o.world = mk3(a.x, a.y, a.z);
         o.uv = mk2(a.w, b.w);
         o.t = mk3(b.x, b.y, b.z);

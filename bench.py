@@ -1,16 +1,23 @@
 #!/usr/bin/env python3
 """Headline benchmark: frames/s of the AxiomR draw path on one GB300.
 
-A step is one frame as the reference renderer produces it (src/renderer.cpp:124-126):
-clearColor + clearDepth + drawMesh of the workload, through the C ABI.
+A frame is what the reference renderer produces per mesh (src/renderer.cpp:124-126):
+clearColor + clearDepth + drawMesh, through the C ABI.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload heightfield|sphere|soup]
+                    [--workload batch|heightfield|sphere|soup] [--no-autotune]
+
+Default workload `batch`: a step renders the 512 draws of the mixed batch, each into its
+own framebuffer, with the batched form (one persistent launch, clears fused, replayed from
+a CUDA graph, raster parameter autotuned per density class); the plain per-draw path on
+the same draws is timed beside it (`plain`, `batched_vs_plain`). The single-draw workloads
+(`heightfield`, `sphere`, `soup`) time one frame per step through the per-draw path.
 
 `value` is frames/s with every input resident in HBM; L2 is flushed (a 256 MiB write) before
 each timed step and each step is timed with CUDA events on the library's stream. `e2e` is
-the same metric with the mesh arrays and texture uploaded from pinned host memory and the
-framebuffer (colour and depth) read back every step, all inside the timed region.
+the same metric with the step's inputs sent from host memory and every framebuffer
+(colour and depth) read back to pinned memory, all inside the timed region (batch: the
+draw table through axr_draw_batch; single draws: mesh arrays and texture from pinned memory).
 `--impl reference` times the CPU restatement of the reference's TiledPipeline (oracle/port,
 all host threads) on the same workload instead. With N > 1 (torchrun), every rank renders
 its own replica of the workload (the path has no cross-GPU exchange); value is the total.
@@ -42,7 +49,11 @@ WORKLOADS = {
     "sphere": (W.sphere_scene, "UV sphere 64x32 (3,968 triangles), 256^2 RGBA8 noise texture, Blinn-Phong, "
                                "camera at distance 3, 512x512"),
     "soup": (W.soup_scene, "200,000 screen-space triangles (edges 0.5-4 px, depths 0.1-100), Gouraud, 3840x2160"),
+    "batch": (W.batch_scenes, "512 draws, each a UV sphere with segments log-uniform 8x4..256x128 (48..65,024 "
+                              "triangles), resolution uniform from {256^2, 512^2, 1024^2, 1920x1080}, camera on a "
+                              "random orbit at distance 2-6, one of 8 1024^2 RGBA8 noise textures, Blinn-Phong"),
 }
+BATCH_REF_SAMPLE = 16  # draws of the mixed batch the CPU arms render per step (every 32nd)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -52,7 +63,10 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="heightfield")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch")
+    ap.add_argument("--no-autotune", action="store_true", help="batch: plan with the default tuning table")
+    ap.add_argument("--draws", type=int, default=512, help="batch: number of draws (a smaller batch for profiling)")
+    ap.add_argument("--scale", type=float, default=1.0, help="batch: framebuffer size scale (profiling)")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -68,7 +82,7 @@ class Dist:
         if self.world > 1:
             import torch.distributed as dist
 
-            backend = "nccl" if self._cuda() else "gloo"
+            backend = os.environ.get("AXR_DIST_BACKEND") or ("nccl" if self._cuda() else "gloo")
             if backend == "nccl":
                 import torch
 
@@ -417,8 +431,242 @@ def run_ours(args, dist: Dist):
     return out, scene
 
 
+def timed_steps(stream, flush, steps: int, body):
+    """K steps of `body`, each bracketed by CUDA events on the library stream after an L2
+    flush (outside the events); returns per-step milliseconds."""
+    import torch
+
+    evs = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        body()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def batch_algo_bytes(scenes, frags: float) -> float:
+    """Algorithmic bytes of one mixed-batch step: per draw the vertex attributes read
+    (position 12 + normal 12 + uv 8), the indices (12 per face), one colour + one depth
+    write per pixel, and min(texture bytes, 4 per covered fragment) summed over draws
+    (covered fragments split by faces)."""
+    total_faces = sum(int(sc.mesh.indices.shape[0]) for sc in scenes)
+    b = 0.0
+    for sc in scenes:
+        V, F = sc.mesh.positions.shape[0], sc.mesh.indices.shape[0]
+        tex = sum(int(t.nbytes) for m in sc.mesh.materials for t in (m.diffuse,) if t is not None)
+        b += 32.0 * V + 12.0 * F + 8.0 * sc.width * sc.height + min(tex, 4.0 * frags * F / max(1, total_faces))
+    return b
+
+
+def run_batch(args, dist: Dist):
+    """The mixed batch: 512 draws into 512 framebuffers per step, batched form (one
+    persistent launch, replayed from a CUDA graph) against the plain per-draw path (clear,
+    clear, drawMesh per draw, also replayed from a CUDA graph)."""
+    import torch
+
+    from axiomr_gb300 import api
+
+    desc = WORKLOADS["batch"][1]
+    scenes = W.batch_scenes(count=args.draws, resolution_scale=args.scale)
+    if args.draws != 512 or args.scale != 1.0:
+        desc += f" [reduced: first {args.draws} draws, framebuffers scaled by {args.scale}]"
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    ctx = api.Context(dev)
+    lib = ctx.lib
+    textures, meshes = {}, {}
+    draws = api.batch_draws(ctx, scenes, textures, meshes)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    n = len(draws)
+
+    # ---- autotune the per-class raster parameter on this batch, then plan it
+    tuning = ctx.tuning() if args.no_autotune else api.autotune(ctx, draws, repeats=2)
+    batch = api.Batch(ctx, draws)
+    info = batch.info()
+    graph = api.Graph(ctx).begin()
+    batch.launch()
+    graph.end()
+
+    # ---- plain per-draw path, recorded once into a graph as well
+    ctx.reserve(max(int(sc.mesh.indices.shape[0]) for sc in scenes))
+    pipe = api.TiledPipeline(ctx)
+    plain_graph = api.Graph(ctx).begin()
+    for d in draws:
+        d.framebuffer.clearColor(*d.clear_color)
+        d.framebuffer.clearDepth(d.clear_depth)
+        pipe.setCamera(d.camera)
+        pipe.setFramebuffer(d.framebuffer)
+        pipe.setShader(d.shader)
+        pipe.drawMesh(d.model, d.mesh)
+    plain_graph.end()
+    launches0 = ctx.profile()["kernel_launches"]
+    for d in draws[:1]:
+        pipe.setCamera(d.camera)
+        pipe.setFramebuffer(d.framebuffer)
+        pipe.setShader(d.shader)
+        d.framebuffer.clearColor(*d.clear_color)
+        d.framebuffer.clearDepth(d.clear_depth)
+        pipe.drawMesh(d.model, d.mesh)
+    plain_launches_per_draw = ctx.profile()["kernel_launches"] - launches0  # clears included
+    ctx.sync()
+
+    # statistics of one batched step
+    ctx.stats(True)
+    ctx.stats()
+    batch.launch()
+    st = ctx.stats()
+    ctx.stats(False)
+
+    for _ in range(max(3, args.warmup)):
+        graph.launch()
+        plain_graph.launch()
+    ctx.sync()
+
+    sampler = ClockSampler(dev)
+    dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    step_ms = timed_steps(stream, flush, args.steps, graph.launch)
+    dist.barrier()
+    sampler.stop()
+    plain_ms = timed_steps(stream, flush, args.steps, plain_graph.launch)
+    # the plain path as a host loop of per-draw calls (no graph), for reference
+    eager_ms = timed_steps(stream, flush, max(3, args.steps // 4), lambda: [
+        (d.framebuffer.clearColor(*d.clear_color), d.framebuffer.clearDepth(d.clear_depth), pipe.setCamera(d.camera),
+         pipe.setFramebuffer(d.framebuffer), pipe.setShader(d.shader), pipe.drawMesh(d.model, d.mesh))
+        for d in draws])
+    ctx.sync()
+    total_ms = dist.max(float(sum(step_ms)))
+    value = n * len(step_ms) * dist.world / (total_ms / 1e3)
+    plain_value = n * len(plain_ms) / (sum(plain_ms) / 1e3)
+    eager_value = n * len(eager_ms) / (sum(eager_ms) / 1e3)
+
+    # ---- end to end: per step the draw table goes up from the host (one-shot batch entry
+    # point) and every framebuffer (colour + depth) comes back to pinned host memory
+    keep = []
+    outs = []
+    for d in draws:
+        w, h = d.framebuffer.width, d.framebuffer.height
+        outs.append((pinned_like(lib, np.zeros((h, w, 4), np.uint8), keep),
+                     pinned_like(lib, np.zeros((h, w), np.float32), keep)))
+    d2h = sum(a.nbytes + b.nbytes for a, b in outs)
+    h2d = n * C.sizeof(api.DrawDesc)
+
+    def e2e_step():
+        api.draw_batch(ctx, draws)
+        for d, (hb, hd) in zip(draws, outs):
+            rc = lib.axr_framebuffer_read_async(ctx.handle, d.framebuffer.handle, hb.ctypes.data, hd.ctypes.data)
+            if rc != 0:
+                raise RuntimeError("axr_framebuffer_read_async failed")
+
+    for _ in range(2):
+        e2e_step()
+    ctx.sync()
+    l0 = ctx.profile()["kernel_launches"]
+    e2e_ms = timed_steps(stream, flush, max(3, args.steps // 2), e2e_step)
+    ctx.sync()
+    e2e_launches = (ctx.profile()["kernel_launches"] - l0) / max(1, len(e2e_ms))
+    e2e_value = n * len(e2e_ms) * dist.world / (dist.max(float(sum(e2e_ms))) / 1e3)
+    for p in keep:
+        lib.axr_host_free(p)
+
+    hbm_peak, peak_kind = measured_peaks()
+    ms = total_ms / len(step_ms)
+    frags = float(st["fragments"])
+    algo = batch_algo_bytes(scenes, frags)
+    achieved = algo / (ms * 1e-3) / 1e9
+    faces = info["faces"]
+    out = {
+        "metric": "frames/s", "value": round(value, 2), "unit": "frames/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
+        "config": {"workload": f"batch: {desc}", "form": "batched: one persistent cooperative launch per step "
+                   "(clears fused), replayed from a CUDA graph",
+                   "frames_per_step": n, "l2": "flushed before every timed step (256 MiB write, outside the events)",
+                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
+                   "tuning_small_max_pixels": tuning},
+        "gfrag_per_s": round(frags * value / n / 1e9, 3),
+        "mtri_per_s": round(faces * value / n / 1e6, 2),
+        "fragments_per_step": int(frags), "triangles_per_step": int(st["triangles"]), "faces_per_step": int(faces),
+        "pixels_per_step": int(info["pixels"]),
+        "plain": {"value": round(plain_value, 2), "unit": "frames/s", "ms_per_step": round(sum(plain_ms) / len(plain_ms), 4),
+                  "form": "per draw: clearColor, clearDepth, drawMesh (9 launches), replayed from a CUDA graph",
+                  "launches_per_draw": int(plain_launches_per_draw)},
+        "plain_eager": {"value": round(eager_value, 2), "unit": "frames/s",
+                        "form": "the same per-draw calls issued from the Python host loop"},
+        "batched_vs_plain": round(value / plain_value, 3),
+        "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "path": "axr_draw_batch (draw table from the host) + colour and depth read-back of all 512 "
+                        "framebuffers into pinned memory; meshes and textures resident",
+                "gpu_launches_per_step": e2e_launches},
+        "gpu_launches": int(info["launches"]) * len(step_ms),
+        "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": round(achieved, 1), "peak": hbm_peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                     "traffic": profiled_traffic("batch_kernel", "batch"), "algorithmic_bytes": algo,
+                     "launch_us": round(ms * 1e3, 2)},
+        "clocks": sampler.summary(),
+    }
+    graph.close()
+    plain_graph.close()
+    batch.close()
+    ctx.close()
+    return out, scenes
+
+
+def cpu_batch_sample(scenes, budget_s: float, steps: int):
+    """The CPU restatement of the reference pipeline (oracle/port) on every 32nd draw of the
+    mixed batch, all host threads; frames/s over those draws (clears included, as the
+    reference renderer's frame)."""
+    from oracle import Oracle
+
+    port = Oracle("port")
+    threads = os.cpu_count() or 1
+    sample = scenes[:: max(1, len(scenes) // BATCH_REF_SAMPLE)][:BATCH_REF_SAMPLE]
+    vps = [port.camera(sc.camera)[2] for sc in sample]
+
+    def step():
+        for sc, vp in zip(sample, vps):
+            port.draw(sc, vp, threads=threads)
+
+    t0 = time.perf_counter()
+    step()  # warm-up, also sizes the run
+    t1 = time.perf_counter() - t0
+    reps = max(1, min(steps, int(budget_s / max(t1, 1e-6))))
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t)
+    value = len(sample) * len(times) / sum(times)
+    return value, threads, times, (f"{reps} x {len(sample)} draws (every {len(scenes) // len(sample)}th draw of the "
+                                   f"batch) on {threads} host threads ({os.uname().machine})")
+
+
 def run_reference(args, dist: Dist):
     make, desc = WORKLOADS[args.workload]
+    if args.workload == "batch":
+        scenes = make()
+        value, threads, times, sample = cpu_batch_sample(scenes, 150.0, args.steps)
+        return {
+            "metric": "frames/s", "value": round(value, 4), "unit": "frames/s", "n_gpus": dist.world,
+            "steps": len(times), "warmup": 1, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
+            "config": {"workload": f"batch: {desc}", "form": "reference CPU TiledPipeline (C restatement), "
+                       "one drawMesh per draw"},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     scene = make()
     from oracle import Oracle
 
@@ -468,6 +716,15 @@ def main():
         if args.impl == "reference":
             if dist.rank == 0:
                 print(json.dumps(run_reference(args, dist)), flush=True)
+            return
+        if args.workload == "batch":
+            out, scenes = run_batch(args, dist)
+            if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+                value, threads, times, sample = cpu_batch_sample(scenes, args.cpu_budget_s, args.steps)
+                out["cpu_baseline"] = {"value": round(value, 4), "unit": "frames/s", "cores": threads,
+                                       "kind": "port", "sample": sample}
+            if dist.rank == 0:
+                print(json.dumps(out), flush=True)
             return
         out, scene = run_ours(args, dist)
         if dist.rank == 0:

@@ -199,23 +199,74 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
 axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
 
 /* ------------------------------------------------------------------ batched form
- * Many independent draws (each with its own framebuffer, camera, shader and mesh) in
- * one persistent launch over a shared work queue; no reference counterpart (the
- * reference issues one drawMesh per mesh). Framebuffers must be distinct within a
- * batch. */
+ * No reference counterpart: the reference renders one mesh per drawMesh call, each a full
+ * pass of its pipeline (src/tiled_pipeline.cpp:143-322; src/renderer.cpp:16-19). A batch
+ * is many independent draws, each with its own mesh, camera, shader, model matrix and
+ * framebuffer, rendered by one persistent cooperative kernel launch per shader kind present
+ * in the batch. Every draw's result is the one axr_draw_mesh gives for it (after the
+ * optional clears, which are fused into the draw's tile pass). The framebuffers of a batch
+ * must be distinct. */
+#define AXR_DRAW_CLEAR_COLOR 1u /* Framebuffer::clearColor before the draw */
+#define AXR_DRAW_CLEAR_DEPTH 2u /* Framebuffer::clearDepth before the draw */
+
 typedef struct axr_draw_desc {
     const axr_mesh* mesh;
     axr_framebuffer* framebuffer;
     float model[16];
     axr_camera_desc camera;
     axr_shader_desc shader;
+    uint32_t clear_flags;   /* AXR_DRAW_CLEAR_* */
+    uint8_t clear_rgba[4];  /* clearColor(Color{r, g, b, a}) */
+    float clear_depth;      /* clearDepth(value); the reference default is +inf */
 } axr_draw_desc;
 
+typedef struct axr_batch axr_batch;
+
+/* Plan a batch: checks the draws, assigns each draw the raster parameters of its density
+ * class from the context's tuning table, uploads the draw table and reserves the batch's
+ * device scratch (vertex caches of all draws, shared large-triangle lists). Returns after
+ * the upload. Meshes, framebuffers and textures must outlive the batch. */
+axr_status axr_batch_create(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch** out);
+/* Enqueue the planned batch on the context stream (per shader kind: a counter reset and
+ * one cooperative launch). Allocates nothing and reads no host memory, so it can be
+ * recorded into a CUDA graph (axr_graph_begin / axr_graph_end) and replayed. */
+axr_status axr_batch_launch(axr_context* ctx, axr_batch* batch);
+void axr_batch_destroy(axr_context* ctx, axr_batch* batch);
+
+typedef struct axr_batch_info {
+    uint32_t draws;
+    uint32_t launches;        /* cooperative launches per axr_batch_launch (shader kinds) */
+    uint64_t vertices;        /* vertices of all draws */
+    uint64_t faces;           /* faces in draw order of all draws */
+    uint64_t pixels;          /* framebuffer pixels of all draws */
+    uint64_t tiles;           /* 16x16 tiles of all draws */
+    uint64_t device_bytes;    /* device memory held by the batch */
+} axr_batch_info;
+axr_status axr_batch_get_info(const axr_batch* batch, axr_batch_info* out);
+
+/* One-shot form: plan into a batch kept by the context (re-used while it is large enough)
+ * and launch it. Not for graph capture (the draw table is uploaded by this call). */
 axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count);
+
+/* Autotuner. A draw's density class is the estimated mean screen area of its front-facing
+ * triangles, from the mesh's bounding sphere projected through its camera: class k covers
+ * [2^(2k-1), 2^(2k+1)) pixels (class 0 below 2, the last class 512 and above). Per class
+ * the tuner picks the largest triangle pixel box rasterised by one thread (larger boxes
+ * go to the warp-per-tile rasteriser) by timing sub-batches of the given draws' classes
+ * with each candidate `repeats` times. The table is the context's; batches planned
+ * afterwards use it. out_small_max_pixels (optional) receives the table. */
+#define AXR_TUNE_CLASSES 6
+axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int32_t count, int32_t repeats,
+                              int32_t out_small_max_pixels[AXR_TUNE_CLASSES]);
+axr_status axr_batch_get_tuning(const axr_context* ctx, int32_t small_max_pixels[AXR_TUNE_CLASSES]);
+axr_status axr_batch_set_tuning(axr_context* ctx, const int32_t small_max_pixels[AXR_TUNE_CLASSES]);
+/* Density class of one draw (the classification the planner uses). */
+int32_t axr_draw_density_class(const axr_draw_desc* draw);
 
 /* ------------------------------------------------------------------ CUDA graphs
  * Record the draws issued on the context between begin and end into a CUDA graph and
- * replay it. Scratch must be reserved (axr_reserve / axr_batch_reserve) beforehand. */
+ * replay it. Per-draw scratch must be reserved (axr_reserve) and batches planned
+ * (axr_batch_create) beforehand. */
 typedef struct axr_graph axr_graph;
 axr_status axr_graph_begin(axr_context* ctx);
 axr_status axr_graph_end(axr_context* ctx, axr_graph** out);
@@ -244,8 +295,9 @@ axr_status axr_stats_read(axr_context* ctx, axr_draw_stats* out); /* synchronise
 
 /* ------------------------------------------------------------------ profiling
  * When enabled, every draw records CUDA events on the context stream between its
- * kernels; axr_profile_read synchronises and returns the summed device time of each stage
- * since the last read, and the number of kernels the library launched. */
+ * kernels, and every batched launch records device timestamps at its grid barriers;
+ * axr_profile_read synchronises and returns the summed device time of each stage since
+ * the last read, and the number of kernels the library launched. */
 typedef struct axr_profile {
     uint32_t draws;          /* draws recorded */
     uint32_t pad_;
@@ -256,6 +308,11 @@ typedef struct axr_profile {
     double shade_ms;         /* per-pixel resolve and shading */
     double clipped_ms;       /* resolve of pixels won by clipped triangles */
     uint64_t kernel_launches;/* all kernels launched on this context since creation */
+    uint64_t batch_launches; /* batched launches timed (including graph replays) */
+    double batch_vertex_ms;  /* batched kernel phases: vertices */
+    double batch_face_ms;    /*   faces (clip, cull, setup, small-triangle raster) */
+    double batch_large_ms;   /*   large-triangle tiles */
+    double batch_tile_ms;    /*   tile pass (key scan, shading, fused clears, write-out) */
 } axr_profile;
 axr_status axr_profile_enable(axr_context* ctx, int32_t enable);
 axr_status axr_profile_read(axr_context* ctx, axr_profile* out);

@@ -1,0 +1,202 @@
+"""Batched form (axr_batch_* / axr_draw_batch): every draw of a batch must give the frame
+that the per-draw path gives for it (the same device functions compute every value, so
+the comparison is exact), and the oracle's frame within the parity bar. Covers the
+fused clears (both, one, none), framebuffers whose width is not a multiple of 4 (no TMA
+tile stores), all shader kinds in one batch (one launch per kind), clipped triangles,
+CUDA-graph replay, the one-shot entry point, the autotuner and argument errors."""
+import numpy as np
+import pytest
+
+from axiomr_gb300 import api
+from axiomr_gb300 import workloads as W
+from axiomr_gb300._lib import AxrError
+from helpers import assert_parity
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(count=24, seed=5, scale=0.25, tex=64):
+    return W.batch_scenes(count=count, seed=seed, tex_size=tex, resolution_scale=scale)
+
+
+def plain_frames(ctx, scenes, draws):
+    """Each draw through the per-draw path into a fresh framebuffer (clear, clear, drawMesh)."""
+    out = []
+    for sc, d in zip(scenes, draws):
+        fb = api.Framebuffer(ctx, sc.width, sc.height)
+        if d.clear_color is not None:
+            fb.clearColor(*d.clear_color)
+        if d.clear_depth is not None:
+            fb.clearDepth(d.clear_depth)
+        pipe = api.TiledPipeline(ctx, d.camera, fb)
+        pipe.setShader(d.shader)
+        pipe.drawMesh(d.model, d.mesh)
+        out.append(fb.read())
+        fb.close()
+    return out
+
+
+def assert_same(got, exp, what):
+    gb, gd = got
+    eb, ed = exp
+    dd = int((np.ascontiguousarray(gd).view(np.uint32) != np.ascontiguousarray(ed).view(np.uint32)).sum())
+    cd = int((gb != eb).any(axis=-1).sum())
+    assert dd == 0 and cd == 0, f"{what}: {dd} depth and {cd} colour pixels differ from the per-draw path"
+
+
+def test_batch_equals_per_draw_path_and_oracle(ctx, port):
+    scenes = small_batch()
+    draws = api.batch_draws(ctx, scenes)
+    batch = api.Batch(ctx, draws)
+    batch.launch()
+    got = [d.framebuffer.read() for d in draws]
+    exp = plain_frames(ctx, scenes, draws)
+    for k, (g, e) in enumerate(zip(got, exp)):
+        assert_same(g, e, f"draw {k}")
+    for k in range(0, len(scenes), 6):  # the oracle on a subset (its CPU time dominates)
+        sc = scenes[k]
+        assert_parity(got[k], port.draw(sc, port.camera(sc.camera)[2]), f"batch draw {k} vs oracle")
+    info = batch.info()
+    assert info["draws"] == len(scenes) and info["launches"] == 1
+    assert info["faces"] == sum(sc.mesh.indices.shape[0] for sc in scenes)
+    batch.close()
+
+
+def test_batch_relaunch_and_graph_replay(ctx):
+    scenes = small_batch(count=12, seed=7)
+    draws = api.batch_draws(ctx, scenes)
+    batch = api.Batch(ctx, draws)
+    batch.launch()
+    first = [d.framebuffer.read() for d in draws]
+    for d in draws:  # scribble, so that the replay has to rewrite everything
+        d.framebuffer.clearColor(9, 9, 9, 9)
+        d.framebuffer.clearDepth(-1.0)
+    g = api.Graph(ctx).begin()
+    batch.launch()
+    g.end()
+    for _ in range(2):
+        g.launch()
+    ctx.sync()
+    for k, d in enumerate(draws):
+        assert_same(d.framebuffer.read(), first[k], f"graph replay draw {k}")
+    g.close()
+    batch.close()
+
+
+def test_one_shot_batch_and_clear_variants(ctx):
+    scenes = small_batch(count=9, seed=11)
+    draws = api.batch_draws(ctx, scenes)
+    # draws 0-2 clear both planes, 3-5 colour only, 6-8 nothing; the framebuffers start
+    # from a known non-clear state
+    for k, d in enumerate(draws):
+        d.framebuffer.clearColor(10, 20, 30, 40)
+        d.framebuffer.clearDepth(0.999)
+        if 3 <= k < 6:
+            d.clear_depth = None
+        elif k >= 6:
+            d.clear_color = None
+            d.clear_depth = None
+    api.draw_batch(ctx, draws)
+    got = [d.framebuffer.read() for d in draws]
+    exp = []
+    for sc, d in zip(scenes, draws):
+        fb = api.Framebuffer(ctx, sc.width, sc.height)
+        fb.clearColor(10, 20, 30, 40)
+        fb.clearDepth(0.999)
+        if d.clear_color is not None:
+            fb.clearColor(*d.clear_color)
+        if d.clear_depth is not None:
+            fb.clearDepth(d.clear_depth)
+        pipe = api.TiledPipeline(ctx, d.camera, fb)
+        pipe.setShader(d.shader)
+        pipe.drawMesh(d.model, d.mesh)
+        exp.append(fb.read())
+    for k in range(len(draws)):
+        assert_same(got[k], exp[k], f"one-shot draw {k}")
+    # a second one-shot batch of another size re-plans into the same context batch
+    api.draw_batch(ctx, draws[:4])
+    ctx.sync()
+
+
+def test_batch_odd_widths_without_tma(ctx):
+    """Widths that are not a multiple of 4 have no tensor map: plain tile stores."""
+    scenes = [W.sphere_scene(width=w, height=h, lon=lon, lat=lon // 2, tex_size=32)
+              for (w, h, lon) in ((250, 131, 24), (97, 203, 40), (33, 17, 8), (1001, 64, 64))]
+    draws = api.batch_draws(ctx, scenes)
+    api.Batch(ctx, draws).launch()
+    got = [d.framebuffer.read() for d in draws]
+    exp = plain_frames(ctx, scenes, draws)
+    for k in range(len(scenes)):
+        assert_same(got[k], exp[k], f"odd width draw {k}")
+
+
+def test_batch_all_shader_kinds(ctx, port):
+    """Flat, Phong, PBR, Blinn-Phong and Gouraud draws in one batch: one launch per kind."""
+    scenes = []
+    for k, kind in enumerate((W.SHADER_FLAT, W.SHADER_PHONG, W.SHADER_PBR, W.SHADER_BLINN_PHONG, W.SHADER_GOURAUD)):
+        if kind == W.SHADER_GOURAUD:
+            sc = W.soup_scene(count=2000, width=128, height=96, seed=20 + k, edge_min=2, edge_max=20,
+                              depth_min=0.5, depth_max=5.0)
+        else:
+            sc = W.sphere_scene(width=128, height=96, lon=32, lat=16, tex_size=32, shader=kind)
+        scenes.append(sc)
+    draws = api.batch_draws(ctx, scenes)
+    batch = api.Batch(ctx, draws)
+    assert batch.info()["launches"] == 5
+    batch.launch()
+    got = [d.framebuffer.read() for d in draws]
+    exp = plain_frames(ctx, scenes, draws)
+    for k, sc in enumerate(scenes):
+        assert_same(got[k], exp[k], f"shader kind {sc.shader.kind}")
+        assert_parity(got[k], port.draw(sc, port.camera(sc.camera)[2]), f"batch shader {sc.shader.kind} vs oracle")
+
+
+def test_batch_clipped_triangles(ctx):
+    """Cameras inside the near/side planes of the spheres exercise the clipped-winner path."""
+    scenes = []
+    for k, dist in enumerate((1.05, 1.3, 1.6)):
+        sc = W.batch_scenes(count=1, seed=5, tex_size=32, resolution_scale=0.25)[0]
+        cam = W.orbit_camera(dist, 10.0 * k, 30.0 * k, sc.width, sc.height)
+        scenes.append(W.Scene(f"clip{k}", sc.mesh, cam, sc.shader, sc.width, sc.height))
+    draws = api.batch_draws(ctx, scenes)
+    api.Batch(ctx, draws).launch()
+    got = [d.framebuffer.read() for d in draws]
+    exp = plain_frames(ctx, scenes, draws)
+    for k in range(len(scenes)):
+        assert_same(got[k], exp[k], f"clipped draw {k}")
+
+
+def test_autotune_table(ctx):
+    scenes = small_batch(count=16, seed=13)
+    draws = api.batch_draws(ctx, scenes)
+    classes = {api.density_class(d) for d in draws}
+    assert all(0 <= c < 6 for c in classes)
+    before = ctx.tuning()
+    table = api.autotune(ctx, draws, repeats=1)
+    assert len(table) == 6 and all(v in (16, 32, 64, 128, 256) for v in table)
+    assert ctx.tuning() == table
+    for c in range(6):
+        if c not in classes:
+            assert table[c] == before[c]
+    # a batch planned with the tuned table gives the same frames
+    batch = api.Batch(ctx, draws)
+    batch.launch()
+    got = [d.framebuffer.read() for d in draws]
+    exp = plain_frames(ctx, scenes, draws)
+    for k in range(len(scenes)):
+        assert_same(got[k], exp[k], f"tuned draw {k}")
+    ctx.set_tuning(before)
+
+
+def test_batch_argument_errors(ctx):
+    scenes = small_batch(count=2, seed=3)
+    draws = api.batch_draws(ctx, scenes)
+    dup = [draws[0], api.Draw(draws[1].mesh, draws[0].framebuffer, draws[1].camera, draws[1].shader)]
+    with pytest.raises(AxrError) as ei:
+        api.Batch(ctx, dup)
+    assert "distinct" in ei.value.message
+    bad = api.Draw(draws[0].mesh, draws[0].framebuffer, draws[0].camera, api.Shader(17))
+    with pytest.raises(AxrError):
+        api.draw_batch(ctx, [bad])
+    api.draw_batch(ctx, [])  # empty batch: nothing to do
+    ctx.sync()
