@@ -57,8 +57,13 @@ class DrawDesc(C.Structure):
                 ("clear_rgba", C.c_uint8 * 4), ("clear_depth", C.c_float)]
 
 
+AXR_BATCH_PERSISTENT = 0
+AXR_BATCH_PHASED = 1
+
+
 class BatchInfo(C.Structure):
-    _fields_ = [("draws", C.c_uint32), ("launches", C.c_uint32), ("vertices", C.c_uint64), ("faces", C.c_uint64),
+    _fields_ = [("draws", C.c_uint32), ("launches", C.c_uint32), ("form", C.c_int32), ("pad_", C.c_uint32),
+                ("vertices", C.c_uint64), ("faces", C.c_uint64),
                 ("pixels", C.c_uint64), ("tiles", C.c_uint64), ("device_bytes", C.c_uint64)]
 
 
@@ -72,6 +77,41 @@ class Profile(C.Structure):
 
 class DrawStats(C.Structure):
     _fields_ = [("triangles", C.c_uint64), ("fragments", C.c_uint64), ("large", C.c_uint64), ("tiles", C.c_uint64)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("memory_budget_bytes", C.c_uint64), ("max_batch", C.c_int32),
+                ("max_inflight", C.c_int32), ("per_request", C.c_int32), ("pad_", C.c_int32)]
+
+
+class ServerMaterial(C.Structure):
+    _fields_ = [("diffuse", C.c_int32), ("bump", C.c_int32), ("metallic", C.c_int32), ("roughness", C.c_int32),
+                ("ao", C.c_int32), ("specular_exponent", C.c_float)]
+
+
+class ServerMeshDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("positions", C.c_void_p), ("uvs", C.c_void_p),
+                ("normals", C.c_void_p), ("tangents", C.c_void_p), ("bitangents", C.c_void_p),
+                ("num_faces", C.c_uint32), ("indices", C.c_void_p), ("num_groups", C.c_uint32),
+                ("groups", C.c_void_p), ("num_materials", C.c_uint32), ("materials", C.c_void_p)]
+
+
+class ServerRequest(C.Structure):
+    _fields_ = [("mesh", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("model", C.c_float * 16),
+                ("camera", CameraDesc), ("shader", ShaderDesc), ("clear_flags", C.c_uint32),
+                ("clear_rgba", C.c_uint8 * 4), ("clear_depth", C.c_float), ("arrival_ns", C.c_uint64),
+                ("out_bgra", C.c_void_p), ("out_depth", C.c_void_p)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_uint32), ("arrival_ns", C.c_uint64),
+                ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64), ("batch_id", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
+                ("uploads", C.c_uint64), ("evictions", C.c_uint64), ("framebuffers", C.c_uint64),
+                ("resident_bytes", C.c_uint64), ("peak_bytes", C.c_uint64)]
 
 
 P = C.c_void_p
@@ -120,6 +160,18 @@ SIGNATURES = {
     "axr_batch_get_tuning": (S, [P, P]),
     "axr_batch_set_tuning": (S, [P, P]),
     "axr_draw_density_class": (C.c_int32, [P]),
+    "axr_batch_set_form": (S, [P, C.c_int32]),
+    "axr_server_create": (S, [P, PP]),
+    "axr_server_destroy": (None, [P]),
+    "axr_server_now_ns": (C.c_uint64, []),
+    "axr_server_add_texture": (S, [P, P, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
+    "axr_server_add_mesh": (S, [P, P, C.POINTER(C.c_int32)]),
+    "axr_server_submit": (S, [P, P, C.POINTER(C.c_uint64)]),
+    "axr_server_wait": (S, [P, C.c_uint64, C.c_int32, P]),
+    "axr_server_get_stats": (S, [P, P]),
+    "axr_server_hold": (S, [P, C.c_int32]),
+    "axr_server_last_error": (C.c_char_p, [P]),
+    "axr_batch_get_form": (C.c_int32, [P]),
     "axr_graph_begin": (S, [P]),
     "axr_graph_end": (S, [P, PP]),
     "axr_graph_launch": (S, [P, P]),

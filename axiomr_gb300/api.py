@@ -11,6 +11,7 @@ Names and argument meaning follow the reference classes:
   Renderer.drawMesh                        src/renderer.cpp:16-19
   Draw, Batch, draw_batch, autotune        the batched form (no reference counterpart)
   Graph                                    CUDA-graph capture and replay of a context's work
+  Server                                   the serving loop (continuous batching, budgeted residency)
 Every call runs the CUDA library; there is no CPU path.
 """
 from __future__ import annotations
@@ -84,6 +85,15 @@ class Context:
         out = (C.c_int32 * AXR_TUNE_CLASSES)()
         check(self.lib.axr_batch_get_tuning(self.handle, out), self.handle)
         return list(out)
+
+    @property
+    def batch_form(self) -> int:
+        """Launch form of batches planned next (AXR_BATCH_PERSISTENT / AXR_BATCH_PHASED)."""
+        return int(self.lib.axr_batch_get_form(self.handle))
+
+    @batch_form.setter
+    def batch_form(self, form: int) -> None:
+        check(self.lib.axr_batch_set_form(self.handle, int(form)), self.handle)
 
     def set_tuning(self, small_max_pixels: Sequence[int]) -> None:
         arr = (C.c_int32 * AXR_TUNE_CLASSES)(*[int(v) for v in small_max_pixels])
@@ -561,3 +571,109 @@ def batch_draws(ctx: Context, scenes, textures: Optional[dict] = None, meshes: O
                         Shader(sh.kind, tuple(sh.light_direction), tuple(sh.light_color)), sc.model,
                         (r, g, b, a) if clear else None, float("inf") if clear else None))
     return out
+
+
+# ---------------------------------------------------------------- serving loop
+class Server:
+    """The C++ serving loop (axr_server): register mesh assets and textures once, submit
+    render requests, wait for their results. Latency is measured on the server clock."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 40 << 30, max_batch: int = 64, max_inflight: int = 2,
+                 per_request: bool = False):
+        self.lib = _lib.load()
+        cfg = _lib.ServerConfig(int(device), int(budget_bytes), int(max_batch), int(max_inflight),
+                                1 if per_request else 0, 0)
+        h = C.c_void_p()
+        st = self.lib.axr_server_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise AxrError(st, self.lib.axr_last_error(None).decode(errors="replace"))
+        self.handle = h
+        self._textures = {}
+
+    def _check(self, st):
+        if st != 0:
+            msg = self.lib.axr_server_last_error(self.handle) or self.lib.axr_last_error(None)
+            raise AxrError(st, msg.decode(errors="replace"))
+
+    def now_ns(self) -> int:
+        return int(self.lib.axr_server_now_ns())
+
+    def add_texture(self, rgba: np.ndarray) -> int:
+        rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+        out = C.c_int32()
+        self._check(self.lib.axr_server_add_texture(self.handle, rgba.ctypes.data, rgba.shape[1], rgba.shape[0],
+                                                    C.byref(out)))
+        return out.value
+
+    def add_mesh(self, mesh) -> int:
+        """Register an axiomr_gb300.workloads.Mesh (its material textures once each)."""
+        def tex(img):
+            if img is None:
+                return -1
+            if id(img) not in self._textures:
+                self._textures[id(img)] = (self.add_texture(img), img)
+            return self._textures[id(img)][0]
+        mats = (_lib.ServerMaterial * max(1, len(mesh.materials)))()
+        for k, m in enumerate(mesh.materials):
+            mats[k] = _lib.ServerMaterial(tex(m.diffuse), tex(m.bump), tex(m.metallic), tex(m.roughness), tex(m.ao),
+                                          float(m.specular_exponent))
+        pos, uv, nrm = _f32(mesh.positions), _f32(mesh.uvs), _f32(mesh.normals)
+        tan = None if mesh.tangents is None else _f32(mesh.tangents)
+        bit = None if mesh.bitangents is None else _f32(mesh.bitangents)
+        idx = np.ascontiguousarray(mesh.indices, dtype=np.uint32)
+        groups = np.ascontiguousarray(mesh.groups, dtype=np.uint32).reshape(-1, 3)
+        d = _lib.ServerMeshDesc(pos.shape[0], pos.ctypes.data, uv.ctypes.data, nrm.ctypes.data, _ptr(tan), _ptr(bit),
+                                idx.shape[0], idx.ctypes.data, groups.shape[0], groups.ctypes.data,
+                                len(mesh.materials), C.cast(mats, C.c_void_p))
+        out = C.c_int32()
+        self._check(self.lib.axr_server_add_mesh(self.handle, C.byref(d), C.byref(out)))
+        return out.value
+
+    def submit(self, mesh_id: int, camera: "Camera", shader: Shader, width: int, height: int, model=None,
+               clear_color=(0, 0, 0, 255), clear_depth: float = float("inf"), out_bgra: Optional[np.ndarray] = None,
+               out_depth: Optional[np.ndarray] = None, arrival_ns: int = 0) -> int:
+        r = _lib.ServerRequest()
+        r.mesh = int(mesh_id)
+        r.width, r.height = int(width), int(height)
+        r.model = (C.c_float * 16)(*_model(model))
+        r.camera = camera.desc()
+        r.shader = shader.desc()
+        flags = 0
+        if clear_color is not None:
+            flags |= AXR_DRAW_CLEAR_COLOR
+            r.clear_rgba = (C.c_uint8 * 4)(*[int(v) for v in clear_color])
+        if clear_depth is not None:
+            flags |= AXR_DRAW_CLEAR_DEPTH
+            r.clear_depth = float(clear_depth)
+        r.clear_flags = flags
+        r.arrival_ns = int(arrival_ns)
+        r.out_bgra = _ptr(out_bgra)
+        r.out_depth = _ptr(out_depth)
+        t = C.c_uint64()
+        self._check(self.lib.axr_server_submit(self.handle, C.byref(r), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> dict:
+        res = _lib.ServerResult()
+        self._check(self.lib.axr_server_wait(self.handle, int(ticket), int(timeout_ms), C.byref(res)))
+        return {k: getattr(res, k) for k, _ in _lib.ServerResult._fields_}
+
+    def hold(self, on: bool = True) -> None:
+        """Stop admitting (requests queue up) / resume admitting the queue as batches."""
+        self._check(self.lib.axr_server_hold(self.handle, 1 if on else 0))
+
+    def stats(self) -> dict:
+        st = _lib.ServerStats()
+        self._check(self.lib.axr_server_get_stats(self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.axr_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -240,6 +240,7 @@ void axr_context_destroy(axr_context* ctx) {
     DeviceGuard g(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : ctx->batch_events) cudaEventDestroy(ev);
     if (ctx->oneshot) {
         free_batch(ctx->oneshot);
         delete ctx->oneshot;
@@ -724,6 +725,16 @@ axr_status axr_profile_read(axr_context* ctx, axr_profile* out) {
     r.batch_face_ms = bp.phase_ns[1] * 1e-6;
     r.batch_large_ms = bp.phase_ns[2] * 1e-6;
     r.batch_tile_ms = bp.phase_ns[3] * 1e-6;
+    for (size_t k = 0; k + 5 <= ctx->batch_events_used; k += 5) {
+        double* out[4] = {&r.batch_vertex_ms, &r.batch_face_ms, &r.batch_large_ms, &r.batch_tile_ms};
+        for (int j = 0; j < 4; ++j) {
+            float ms = 0.f;
+            AXR_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->batch_events[k + j], ctx->batch_events[k + j + 1]));
+            *out[j] += ms;
+        }
+        ++r.batch_launches;
+    }
+    ctx->batch_events_used = 0;
     r.kernel_launches = ctx->launches;
     *out = r;
     return AXR_OK;

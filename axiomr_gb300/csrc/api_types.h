@@ -67,6 +67,7 @@ struct axr_batch {
     void* dev = nullptr;
     size_t bytes = 0;
     std::vector<Launch> launches;
+    int form = 0;  // axr::kForm*
     uint32_t count = 0;
     uint64_t vertices = 0, faces = 0, pixels = 0, tiles = 0;
 };
@@ -105,7 +106,10 @@ struct axr_context {
     // (autotuned), and the reusable plan of axr_draw_batch
     int32_t tune_small[AXR_TUNE_CLASSES] = {64, 64, 64, 64, 64, 64};
     axr_batch* oneshot = nullptr;
-    axr::BatchProfile* batch_prof = nullptr;  // device-side phase timing of batched launches
+    axr::BatchProfile* batch_prof = nullptr;  // device-side phase timing of persistent launches
+    int batch_form = axr::kFormPhased;        // launch form of batches planned next
+    std::vector<cudaEvent_t> batch_events;     // phase events of phased launches (5 per launch)
+    size_t batch_events_used = 0;
     // profiling: per-draw stage events (4 per draw), reused across reads
     bool profile = false;
     std::vector<cudaEvent_t> event_pool;

@@ -34,6 +34,12 @@ constexpr int kBatchWarps = kBatchBlock / 32;
 constexpr int kBatchMinBlocks = 3;  // 256 threads x 3 CTAs: at most 85 registers
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
 
+// Resident 256-thread CTAs per SM the phased tile kernel is compiled for (4: at most 64
+// registers; its shared memory, 36 KB per CTA, allows 6).
+#ifndef AXR_TILE_MIN_BLOCKS
+#define AXR_TILE_MIN_BLOCKS 4
+#endif
+
 static_assert(sizeof(DrawParams) % 16 == 0, "DrawParams is copied as 16-byte words");
 static_assert(offsetof(BatchDraw, p) % 16 == 0, "DrawParams is copied as 16-byte words");
 
@@ -138,261 +144,416 @@ __device__ __forceinline__ void tma_wait_read_1() { asm volatile("cp.async.bulk.
 
 __device__ __forceinline__ void tma_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
-// One 16x16 tile of draw `p` (`dirty`: its flag was set): read its keys, shade the winners,
-// write the tile. The caller skips tiles that are neither dirty nor to be cleared.
-// stage: this warp's staging buffer (colour plane [256] then depth plane [256]);
-// list: this warp's 256-entry pixel list. Returns whether a TMA store was committed.
+// Winner that came out of the clipper: its inputs from the clipper re-run, then the
+// fragment; kept out of line so that the clipper's state does not raise the register count
+// of the tile pass.
 template <int S>
-__device__ bool tile_pass(const DrawParams& p, const UnitInfo& ui, const BatchDraw* bd, uint32_t tile, bool dirty,
-                          uint32_t* stage, uint8_t* list, DevCounters* counters, bool stats) {
+__device__ __noinline__ bool shade_clipped(const DrawParams& p, uint32_t tag, int gx, int gy, float old, uint32_t* bgra,
+                                           float* z) {
+    Screen s;
+    VSOut vo[3];
+    uint32_t material;
+    return clipped_inputs<S>(p, tag, s, vo, material) && shade_pixel<S>(p, gx, gy, material, s, vo, old, *bgra, *z);
+}
+
+// ---- the tile pass, in three steps over one 16x16 tile of draw `p`:
+//   tile_scan    (warp) keys -> pixel lists in shared memory: unclipped winners from the
+//                front of `list`, clipped ones from the back, their tags parked in the
+//                colour staging slots; keys and flag reset; pixels without a key get the
+//                requested clear (staged when both planes are cleared, else written)
+//   shade_winner (thread) one unclipped winner: fragment, merged into the staging slots
+//                or written to the framebuffer
+//   tile_finish  (warp) the clipped winners (rare), then the staged tile out with two
+//                TMA tensor stores (or plain stores when the pitch has no tensor map)
+// `stage` is the tile's staging buffer: colour plane [256] then depth plane [256].
+struct TileCtx {
+    uint32_t tile;
+    int tx, ty;
+    bool clear_c, clear_d, full;
+};
+
+__device__ __forceinline__ TileCtx tile_ctx(const DevTarget& t, const UnitInfo& ui, uint32_t tile) {
+    TileCtx c;
+    c.tile = tile;
+    c.tx = (int)(tile % (uint32_t)t.tiles_x);
+    c.ty = (int)(tile / (uint32_t)t.tiles_x);
+    c.clear_c = (ui.flags & kBatchClearColor) != 0u;
+    c.clear_d = (ui.flags & kBatchClearDepth) != 0u;
+    c.full = c.clear_c && c.clear_d;
+    return c;
+}
+
+// Returns nwin | nclip << 16 (lane-uniform).
+__device__ uint32_t tile_scan(const DrawParams& p, const UnitInfo& ui, const TileCtx& c, bool dirty, uint32_t* stage,
+                              uint8_t* list, DevCounters* counters, bool stats) {
     const DevTarget& t = p.target;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    const bool clear_c = (ui.flags & kBatchClearColor) != 0u, clear_d = (ui.flags & kBatchClearDepth) != 0u;
-    const bool full = clear_c && clear_d;  // every pixel of the tile is rewritten
-    const int tx = (int)(tile % (uint32_t)t.tiles_x), ty = (int)(tile / (uint32_t)t.tiles_x);
     const int lx = lane & 15, ly0 = lane >> 4;
-    const int px = tx * kTile + lx;
+    const int px = c.tx * kTile + lx;
     uint32_t* s_col = stage;
     float* s_dep = reinterpret_cast<float*>(stage + 256);
     const float cd = ui.clear_depth;
     const uint32_t cc = ui.clear_bgra;
-
-    unsigned long long keys[8];
-    unsigned ms[8];
-    uint32_t nwin = 0;
+    uint32_t nwin = 0, nclip = 0;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        const int py = ty * kTile + ly0 + 2 * r;
+        const int ly = ly0 + 2 * r, py = c.ty * kTile + ly, pix = ly * kTile + lx;
         const bool in = px < t.width && py < t.height;
-        keys[r] = (dirty && in) ? t.key[(uint32_t)py * (uint32_t)t.width + (uint32_t)px] : kEmptyKey;
-        if (full) {
-            s_col[(ly0 + 2 * r) * kTile + lx] = cc;
-            s_dep[(ly0 + 2 * r) * kTile + lx] = cd;
+        const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
+        const unsigned long long key = (dirty && in) ? t.key[idx] : kEmptyKey;
+        const bool has = key != kEmptyKey;
+        const bool clipped = has && (((uint32_t)key) & 8u) != 0u;
+        const unsigned mw = __ballot_sync(0xFFFFFFFFu, has && !clipped);
+        const unsigned mc = __ballot_sync(0xFFFFFFFFu, clipped);
+        if (has) {
+            t.key[idx] = kEmptyKey;  // reset for the next draw into this framebuffer
+            s_col[pix] = (uint32_t)key;
+            if (clipped)
+                list[255u - (nclip + (uint32_t)__popc(mc & below))] = (uint8_t)pix;
+            else
+                list[nwin + (uint32_t)__popc(mw & below)] = (uint8_t)pix;
+        } else if (c.full) {
+            s_col[pix] = cc;
+            s_dep[pix] = cd;
+        } else if (in) {
+            if (c.clear_c) t.color[idx] = cc;
+            if (c.clear_d) t.depth[idx] = cd;
         }
+        nwin += (uint32_t)__popc(mw);
+        nclip += (uint32_t)__popc(mc);
     }
-    __syncwarp();
-    // unclipped winners: pixel index into the list, tag parked in the colour staging slot
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const bool has = keys[r] != kEmptyKey;
-        const bool win = has && (((uint32_t)keys[r]) & 8u) == 0u;
-        ms[r] = __ballot_sync(0xFFFFFFFFu, win);
-        if (win) {
-            const int pix = (ly0 + 2 * r) * kTile + lx;
-            list[nwin + (uint32_t)__popc(ms[r] & below)] = (uint8_t)pix;
-            s_col[pix] = (uint32_t)keys[r];
-        }
-        nwin += (uint32_t)__popc(ms[r]);
+    if (dirty && lane == 0) {
+        t.tile_flag[c.tile] = 0u;
+        if (stats) atomicAdd(&counters->stat_tiles, 1ull);
     }
-    __syncwarp();
-    for (uint32_t base = 0; base < nwin; base += 32) {
-        const uint32_t q = base + (uint32_t)lane;
-        uint32_t pix = 0, bgra = cc;
-        float z = cd;
-        bool ok = false;
-        if (q < nwin) {
-            pix = list[q];
-            const uint32_t tag = s_col[pix];
-            const int gx = tx * kTile + (int)(pix & 15u), gy = ty * kTile + (int)(pix >> 4);
-            const size_t idx = (size_t)gy * (size_t)t.width + (size_t)gx;
-            const float old = clear_d ? cd : t.depth[idx];
-            Screen s;
-            VSOut vo[3];
-            const uint32_t material = winner_inputs<S, true>(p, tag, s, vo);
-            ok = shade_pixel<S>(p, gx, gy, material, s, vo, old, bgra, z);
-            if (!full) {
-                if (ok) {
-                    t.color[idx] = bgra;
-                    t.depth[idx] = z;
-                } else {
-                    if (clear_c) t.color[idx] = cc;
-                    if (clear_d) t.depth[idx] = cd;
-                }
-            }
-        }
-        __syncwarp();  // every tag of this round is read before any slot is overwritten
-        if (q < nwin && full) {
-            s_col[pix] = ok ? bgra : cc;
-            s_dep[pix] = ok ? z : cd;
-        }
+    return nwin | (nclip << 16);
+}
+
+// Merge one shaded (or rejected) fragment of pixel `pix` of the tile.
+__device__ __forceinline__ void tile_put(const DevTarget& t, const UnitInfo& ui, const TileCtx& c, uint32_t* stage,
+                                         uint32_t pix, size_t idx, bool ok, uint32_t bgra, float z) {
+    if (c.full) {
+        stage[pix] = ok ? bgra : ui.clear_bgra;
+        reinterpret_cast<float*>(stage + 256)[pix] = ok ? z : ui.clear_depth;
+    } else if (ok) {
+        t.color[idx] = bgra;
+        t.depth[idx] = z;
+    } else {
+        if (c.clear_c) t.color[idx] = ui.clear_bgra;
+        if (c.clear_d) t.depth[idx] = ui.clear_depth;
     }
-    // clipped winners (rare): each lane re-clips its own pixels
+}
+
+template <int S>
+__device__ __forceinline__ void shade_winner(const DrawParams& p, const UnitInfo& ui, const TileCtx& c, uint32_t* stage,
+                                             uint32_t pix) {
+    const DevTarget& t = p.target;
+    const uint32_t tag = stage[pix];
+    const int gx = c.tx * kTile + (int)(pix & 15u), gy = c.ty * kTile + (int)(pix >> 4);
+    const size_t idx = (size_t)gy * (size_t)t.width + (size_t)gx;
+    const float old = c.clear_d ? ui.clear_depth : t.depth[idx];
+    Screen s;
+    VSOut vo[3];
+    const uint32_t material = winner_inputs<S, true>(p, tag, s, vo);
+    uint32_t bgra = 0u;
+    float z = 0.0f;
+    const bool ok = shade_pixel<S>(p, gx, gy, material, s, vo, old, bgra, z);
+    tile_put(t, ui, c, stage, pix, idx, ok, bgra, z);
+}
+
+// Returns whether a TMA store was committed.
+template <int S>
+__device__ bool tile_finish(const DrawParams& p, const UnitInfo& ui, const BatchDraw* bd, const TileCtx& c,
+                            uint32_t* stage, const uint8_t* list, uint32_t nclip) {
+    const DevTarget& t = p.target;
+    const int lane = threadIdx.x & 31;
 #pragma unroll 1
-    for (int r = 0; r < 8; ++r) {
-        if (keys[r] == kEmptyKey || (((uint32_t)keys[r]) & 8u) == 0u) continue;
-        const int gy = ty * kTile + ly0 + 2 * r;
-        const int pix = (ly0 + 2 * r) * kTile + lx;
-        const size_t idx = (size_t)gy * (size_t)t.width + (size_t)px;
-        Screen s;
-        VSOut vo[3];
-        uint32_t material, bgra = cc;
-        float z = cd;
-        const float old = clear_d ? cd : t.depth[idx];
-        const bool ok = clipped_inputs<S>(p, (uint32_t)keys[r], s, vo, material) &&
-                        shade_pixel<S>(p, px, gy, material, s, vo, old, bgra, z);
-        if (full) {
-            s_col[pix] = ok ? bgra : cc;
-            s_dep[pix] = ok ? z : cd;
-        } else if (ok) {
-            t.color[idx] = bgra;
-            t.depth[idx] = z;
-        } else {
-            if (clear_c) t.color[idx] = cc;
-            if (clear_d) t.depth[idx] = cd;
-        }
+    for (uint32_t q = (uint32_t)lane; q < nclip; q += 32) {
+        const uint32_t pix = list[255u - q];
+        const uint32_t tag = stage[pix];
+        const int gx = c.tx * kTile + (int)(pix & 15u), gy = c.ty * kTile + (int)(pix >> 4);
+        const size_t idx = (size_t)gy * (size_t)t.width + (size_t)gx;
+        const float old = c.clear_d ? ui.clear_depth : t.depth[idx];
+        uint32_t bgra = 0u;
+        float z = 0.0f;
+        const bool ok = shade_clipped<S>(p, tag, gx, gy, old, &bgra, &z);
+        tile_put(t, ui, c, stage, pix, idx, ok, bgra, z);
     }
-    // pixels without a key: the requested clear (a full clear is already staged)
-    if (!full && (clear_c || clear_d)) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int py = ty * kTile + ly0 + 2 * r;
-            if (keys[r] != kEmptyKey || px >= t.width || py >= t.height) continue;
-            const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
-            if (clear_c) t.color[idx] = cc;
-            if (clear_d) t.depth[idx] = cd;
-        }
-    }
-    // reset the keys and the flag for the next draw into this framebuffer
-    if (dirty) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r)
-            if (keys[r] != kEmptyKey)
-                t.key[(uint32_t)(ty * kTile + ly0 + 2 * r) * (uint32_t)t.width + (uint32_t)px] = kEmptyKey;
-        if (lane == 0) {
-            t.tile_flag[tile] = 0u;
-            if (stats) atomicAdd(&counters->stat_tiles, 1ull);
-        }
-    }
-    if (!full) return false;
+    if (!c.full) return false;
     __syncwarp();
     if (ui.flags & kBatchTma) {
         tma_fence_smem();  // this lane's shared-memory writes -> visible to the TMA unit
         __syncwarp();
         if (lane == 0) {
-            tma_store_tile(&bd->color_map, s_col, tx * kTile, ty * kTile);
-            tma_store_tile(&bd->depth_map, reinterpret_cast<const uint32_t*>(s_dep), tx * kTile, ty * kTile);
+            tma_store_tile(&bd->color_map, stage, c.tx * kTile, c.ty * kTile);
+            tma_store_tile(&bd->depth_map, stage + 256, c.tx * kTile, c.ty * kTile);
             tma_commit();
         }
         return true;
     }
+    const int lx = lane & 15, ly0 = lane >> 4, px = c.tx * kTile + lx;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        const int py = ty * kTile + ly0 + 2 * r;
+        const int py = c.ty * kTile + ly0 + 2 * r;
         if (px >= t.width || py >= t.height) continue;
         const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
-        t.color[idx] = s_col[(ly0 + 2 * r) * kTile + lx];
-        t.depth[idx] = s_dep[(ly0 + 2 * r) * kTile + lx];
+        t.color[idx] = stage[(ly0 + 2 * r) * kTile + lx];
+        t.depth[idx] = reinterpret_cast<const float*>(stage + 256)[(ly0 + 2 * r) * kTile + lx];
     }
     return false;
 }
 
+// The whole tile pass by one warp (persistent form). Returns whether a TMA store was committed.
+template <int S>
+__device__ bool tile_pass(const DrawParams& p, const UnitInfo& ui, const BatchDraw* bd, uint32_t tile, bool dirty,
+                          uint32_t* stage, uint8_t* list, DevCounters* counters, bool stats) {
+    const TileCtx c = tile_ctx(p.target, ui, tile);
+    const uint32_t n = tile_scan(p, ui, c, dirty, stage, list, counters, stats);
+    const uint32_t nwin = n & 0xFFFFu, nclip = n >> 16;
+    __syncwarp();
+#pragma unroll 1
+    for (uint32_t q = threadIdx.x & 31u; q < nwin; q += 32) shade_winner<S>(p, ui, c, stage, list[q]);
+    __syncwarp();
+    return tile_finish<S>(p, ui, bd, c, stage, list, nclip);
+}
+
+// ---- phase bodies, shared by the persistent and the phased forms
+template <int S>
+__device__ __forceinline__ void vertex_unit(const DrawParams& p, const UnitInfo& ui) {
+    const uint32_t i = ui.local * kVertUnit + threadIdx.x;
+    if (i < p.mesh.num_vertices) vertex_one<S>(p, i);
+}
+
+// kCoherent: the vertex cache was written earlier in the same launch
+template <bool kCoherent>
+__device__ __forceinline__ void face_unit(const DrawParams& p, const UnitInfo& ui, DevCounters* c, bool stats) {
+    GeomStats st = {0, 0, 0};
+    uint32_t single_tile = kNoTile;
+    const uint32_t o = ui.local * kFaceUnit + threadIdx.x;
+    if (o < p.mesh.num_drawn) geometry_one<kCoherent>(p, o, st, single_tile);
+    geometry_warp_tail(p.target, c, stats, st, single_tile);
+}
+
+// Large-triangle tile items of all draws, strided over every warp of the grid (items are
+// alike, 256 pixels each, so a static split balances without a shared counter).
+__device__ __forceinline__ void large_items(const BatchParams& bp, bool stats) {
+    const int lane = threadIdx.x & 31;
+    DevCounters* c = bp.counters;
+    const uint32_t n_items = min(ld_acquire(&c->item_count), bp.item_cap);
+    const uint32_t n_tris = min(ld_acquire(&c->large_count), bp.large_cap);
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    uint32_t frags = 0;
+    for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += warps) {
+        const LargeItem item = bp.items[it];
+        if (item.tri >= n_tris) continue;  // reserved slot of a triangle rasterised elsewhere
+        const DevTarget t = bp.draws[bp.large_draw[item.tri]].p.target;
+        Edges e;
+        uint32_t tag;
+        load_large(&bp.large[item.tri], e, tag);
+        large_tile(t, e, tag, item.tile, frags);
+    }
+    if (stats) {
+        const uint32_t f = __reduce_add_sync(0xFFFFFFFFu, frags);
+        if (lane == 0 && f) atomicAdd(&c->stat_fragments, (unsigned long long)f);
+    }
+}
+
+// Both planes of a tile without keys set to the clear values with direct stores: 8 pixels
+// of one row per lane (two 16-byte stores per plane) when the tile lies inside a
+// framebuffer whose width is a multiple of 4, one pixel per store otherwise.
+__device__ __forceinline__ void clear_tile(const DevTarget& t, uint32_t tile, uint32_t cc, float cd) {
+    const int lane = threadIdx.x & 31;
+    const int tx = (int)(tile % (uint32_t)t.tiles_x), ty = (int)(tile / (uint32_t)t.tiles_x);
+    const int x0 = tx * kTile, y0 = ty * kTile;
+    if ((t.width & 3) == 0 && x0 + kTile <= t.width && y0 + kTile <= t.height) {
+        const int py = y0 + (lane >> 1), px = x0 + 8 * (lane & 1);
+        const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
+        const uint4 c4 = make_uint4(cc, cc, cc, cc);
+        const float4 d4 = make_float4(cd, cd, cd, cd);
+        uint4* c = reinterpret_cast<uint4*>(t.color + idx);
+        float4* d = reinterpret_cast<float4*>(t.depth + idx);
+        c[0] = c4;
+        c[1] = c4;
+        d[0] = d4;
+        d[1] = d4;
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int px = x0 + (lane & 15), py = y0 + (lane >> 4) + 2 * r;
+        if (px >= t.width || py >= t.height) continue;
+        const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
+        t.color[idx] = cc;
+        t.depth[idx] = cd;
+    }
+}
+
+// A warp's tiles of a tile unit: their flags with one load per lane, then tile_pass on each
+// tile that is dirty or to be cleared. *sbuf alternates the warp's two staging buffers.
+template <int S>
+__device__ __forceinline__ void tile_unit(const BatchParams& bp, const DrawParams& p, const UnitInfo& ui,
+                                          uint32_t* stage2, uint8_t* list, int* sbuf, bool stats) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tpw = bp.tiles_per_warp;
+    const uint32_t ntiles = (uint32_t)p.target.tiles_x * (uint32_t)p.target.tiles_y;
+    const uint32_t first = (ui.local * kUnitWarps + (uint32_t)warp) * tpw;
+    const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
+    const bool flag = (uint32_t)lane < tpw && first + (uint32_t)lane < ntiles &&
+                      ld_volatile(&p.target.tile_flag[first + (uint32_t)lane]) != 0u;
+    const unsigned dirty = __ballot_sync(0xFFFFFFFFu, flag);
+    const bool full_clear = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth);
+    for (uint32_t j = 0; j < tpw; ++j) {
+        const uint32_t tile = first + j;
+        if (tile >= ntiles) break;
+        const bool d = (dirty >> j) & 1u;
+        if (!d && !clears) continue;
+        if (!d && full_clear) {
+            clear_tile(p.target, tile, ui.clear_bgra, ui.clear_depth);
+            continue;
+        }
+        // the store issued from this buffer two tiles ago must have read it
+        if (lane == 0) tma_wait_read_1();
+        __syncwarp();
+        if (tile_pass<S>(p, ui, &bp.draws[ui.draw], tile, d, stage2 + 512 * *sbuf, list, bp.counters, stats))
+            *sbuf ^= 1;
+    }
+}
+
+// ---- persistent form: one cooperative launch, phases behind grid barriers
 template <int S>
 __global__ void __launch_bounds__(kBatchBlock, kBatchMinBlocks) batch_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ __align__(16) DrawParams s_p[2];
     __shared__ UnitInfo s_u[2];
-    __shared__ __align__(128) uint32_t s_stage[kBatchWarps][2][512];  // warp, buffer, colour|depth
+    __shared__ __align__(128) uint32_t s_stage[kBatchWarps][2 * 512];  // warp: 2 x (colour | depth)
     __shared__ uint8_t s_list[kBatchWarps][256];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stats = bp.collect_stats != 0;
-
     BatchProfile* prof = bp.prof;
     if (prof && blockIdx.x == 0 && threadIdx.x == 0) prof->start = global_ns();
     const uint32_t face_base = bp.vert_units, tile_base = bp.vert_units + bp.face_units;
-
-    // ---- phase 1: vertices
     int buf = 0;
     for (uint32_t u = blockIdx.x; u < bp.vert_units; u += gridDim.x, buf ^= 1) {
         stage_unit(bp, u, &s_p[buf], &s_u[buf]);
         __syncthreads();
-        const DrawParams& p = s_p[buf];
-        const uint32_t i = s_u[buf].local * kVertUnit + threadIdx.x;
-        if (i < p.mesh.num_vertices) vertex_one<S>(p, i);
+        vertex_unit<S>(s_p[buf], s_u[buf]);
     }
     if (!grid_barrier(bp.counters, prof, 0)) return;
-
-    // ---- phase 2: faces
     for (uint32_t u = blockIdx.x; u < bp.face_units; u += gridDim.x, buf ^= 1) {
         stage_unit(bp, face_base + u, &s_p[buf], &s_u[buf]);
         __syncthreads();
-        const DrawParams& p = s_p[buf];
-        GeomStats st = {0, 0, 0};
-        uint32_t single_tile = kNoTile;
-        const uint32_t o = s_u[buf].local * kFaceUnit + threadIdx.x;
-        if (o < p.mesh.num_drawn) geometry_one<true>(p, o, st, single_tile);
-        geometry_warp_tail(p.target, bp.counters, stats, st, single_tile);
+        face_unit<true>(s_p[buf], s_u[buf], bp.counters, stats);
     }
     if (!grid_barrier(bp.counters, prof, 1)) return;
-
-    // ---- phase 3: large-triangle tiles of all draws
-    {
-        DevCounters* c = bp.counters;
-        const uint32_t n_items = min(ld_acquire(&c->item_count), bp.item_cap);
-        const uint32_t n_tris = min(ld_acquire(&c->large_count), bp.large_cap);
-        uint32_t frags = 0;
-        for (;;) {
-            uint32_t first = 0;
-            if (lane == 0) first = atomicAdd(&c->item_head, kItemsPerGrab);
-            first = __shfl_sync(0xFFFFFFFFu, first, 0);
-            if (first >= n_items) break;
-            const uint32_t last = min(first + kItemsPerGrab, n_items);
-            for (uint32_t it = first; it < last; ++it) {
-                const LargeItem item = bp.items[it];
-                if (item.tri >= n_tris) continue;  // reserved slot of a triangle rasterised elsewhere
-                const DevTarget t = bp.draws[bp.large_draw[item.tri]].p.target;
-                Edges e;
-                uint32_t tag;
-                load_large(&bp.large[item.tri], e, tag);
-                large_tile(t, e, tag, item.tile, frags);
-            }
-        }
-        if (stats) {
-            const uint32_t f = __reduce_add_sync(0xFFFFFFFFu, frags);
-            if (lane == 0 && f) atomicAdd(&c->stat_fragments, (unsigned long long)f);
-        }
-    }
+    large_items(bp, stats);
     if (!grid_barrier(bp.counters, prof, 2)) return;
-
-    // ---- phase 4: tiles (key scan, shading, fused clear, tile write-out); each warp takes
-    // 8 consecutive tiles of the unit, their flags read with one load per lane
     int sbuf = 0;
     for (uint32_t u = blockIdx.x; u < bp.tile_units; u += gridDim.x, buf ^= 1) {
         stage_unit(bp, tile_base + u, &s_p[buf], &s_u[buf]);
         __syncthreads();
-        const DrawParams& p = s_p[buf];
-        const UnitInfo& ui = s_u[buf];
-        const uint32_t ntiles = (uint32_t)p.target.tiles_x * (uint32_t)p.target.tiles_y;
-        const uint32_t first = ui.local * kTileUnit + (uint32_t)warp * kTilesPerWarp;
-        const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
-        const bool flag = lane < (int)kTilesPerWarp && first + (uint32_t)lane < ntiles &&
-                          ld_volatile(&p.target.tile_flag[first + (uint32_t)lane]) != 0u;
-        const unsigned dirty = __ballot_sync(0xFFFFFFFFu, flag);
-        for (uint32_t j = 0; j < kTilesPerWarp; ++j) {
-            const uint32_t tile = first + j;
-            if (tile >= ntiles) break;
-            const bool d = (dirty >> j) & 1u;
-            if (!d && !clears) continue;
-            // the store issued from this buffer two tiles ago must have read it
-            if (lane == 0) tma_wait_read_1();
-            __syncwarp();
-            if (tile_pass<S>(p, ui, &bp.draws[ui.draw], tile, d, s_stage[warp][sbuf], s_list[warp], bp.counters,
-                             stats))
-                sbuf ^= 1;
-        }
+        tile_unit<S>(bp, s_p[buf], s_u[buf], s_stage[warp], s_list[warp], &sbuf, stats);
     }
     if (lane == 0) tma_wait_all();
     if (prof) profile_exit(prof);
 }
 
+// ---- phased form: one launch per phase, one CTA per work unit (large: persistent warps)
 template <int S>
-cudaError_t launch_batch_s(const BatchParams& bp, int num_sms, cudaStream_t stream, uint64_t* launches) {
+__global__ void __launch_bounds__(kBatchBlock) batch_vertex_kernel(const __grid_constant__ BatchParams bp) {
+    __shared__ __align__(16) DrawParams s_p;
+    __shared__ UnitInfo s_u;
+    stage_unit(bp, blockIdx.x, &s_p, &s_u);
+    __syncthreads();
+    vertex_unit<S>(s_p, s_u);
+}
+
+__global__ void __launch_bounds__(kBatchBlock, 5) batch_face_kernel(const __grid_constant__ BatchParams bp) {
+    __shared__ __align__(16) DrawParams s_p;
+    __shared__ UnitInfo s_u;
+    stage_unit(bp, bp.vert_units + blockIdx.x, &s_p, &s_u);
+    __syncthreads();
+    face_unit<false>(s_p, s_u, bp.counters, bp.collect_stats != 0);
+}
+
+__global__ void __launch_bounds__(kBatchBlock) batch_large_kernel(const __grid_constant__ BatchParams bp) {
+    large_items(bp, bp.collect_stats != 0);
+}
+
+// Tile pass of the phased form: one CTA per 8 tiles (one per warp). Each warp scans its
+// tile, then all 256 threads shade the CTA's winners together (balanced across the eight
+// tiles), then each warp finishes its tile.
+template <int S>
+__global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_kernel(const __grid_constant__ BatchParams bp) {
+    __shared__ __align__(16) DrawParams s_p;
+    __shared__ UnitInfo s_u;
+    __shared__ __align__(128) uint32_t s_stage[kBatchWarps][512];
+    __shared__ uint8_t s_list[kBatchWarps][256];
+    __shared__ uint32_t s_n[kBatchWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool stats = bp.collect_stats != 0;
+    stage_unit(bp, bp.vert_units + bp.face_units + blockIdx.x, &s_p, &s_u);
+    __syncthreads();
+    const DrawParams& p = s_p;
+    const UnitInfo& ui = s_u;
+    const uint32_t ntiles = (uint32_t)p.target.tiles_x * (uint32_t)p.target.tiles_y;
+    const uint32_t tile = ui.local * kUnitWarps + (uint32_t)warp;
+    const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
+    const bool full = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth);
+    const TileCtx c = tile_ctx(p.target, ui, tile);
+    bool active = false;  // this warp's tile goes through the staged pass
+    uint32_t n = 0;
+    if (tile < ntiles) {
+        const bool dirty = __shfl_sync(0xFFFFFFFFu, lane == 0 ? ld_volatile(&p.target.tile_flag[tile]) : 0u, 0) != 0u;
+        if (!dirty && full) {
+            clear_tile(p.target, tile, ui.clear_bgra, ui.clear_depth);
+        } else if (dirty || clears) {
+            active = true;
+            n = tile_scan(p, ui, c, dirty, s_stage[warp], s_list[warp], bp.counters, stats);
+        }
+    }
+    if (lane == 0) s_n[warp] = n & 0xFFFFu;
+    __syncthreads();
+    uint32_t pre[kBatchWarps + 1];
+    pre[0] = 0;
+#pragma unroll
+    for (int w = 0; w < kBatchWarps; ++w) pre[w + 1] = pre[w] + s_n[w];
+    for (uint32_t q = threadIdx.x; q < pre[kBatchWarps]; q += kBatchBlock) {
+        int w = 0;
+#pragma unroll
+        for (int k = 1; k < kBatchWarps; ++k) w += q >= pre[k] ? 1 : 0;
+        const TileCtx cw = tile_ctx(p.target, ui, ui.local * kUnitWarps + (uint32_t)w);
+        shade_winner<S>(p, ui, cw, s_stage[w], s_list[w][q - pre[w]]);
+    }
+    __syncthreads();
+    if (active) tile_finish<S>(p, ui, &bp.draws[ui.draw], c, s_stage[warp], s_list[warp], n >> 16);
+    if (lane == 0) tma_wait_all();
+}
+
+template <int S>
+cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, cudaEvent_t* ev,
+                           uint64_t* launches) {
+    cudaError_t e = cudaMemsetAsync(bp.counters, 0, kBatchCountersReset, stream);
+    if (e != cudaSuccess) return e;
+    if (form == kFormPhased) {
+        auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], stream) : cudaSuccess; };
+        if ((e = mark(0)) != cudaSuccess) return e;
+        if (bp.vert_units) batch_vertex_kernel<S><<<bp.vert_units, kBatchBlock, 0, stream>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1)) != cudaSuccess) return e;
+        if (bp.face_units) batch_face_kernel<<<bp.face_units, kBatchBlock, 0, stream>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(2)) != cudaSuccess) return e;
+        if (bp.face_units) batch_large_kernel<<<(unsigned)num_sms * 5u, kBatchBlock, 0, stream>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(3)) != cudaSuccess) return e;
+        if (bp.tile_units) batch_tile_kernel<S><<<bp.tile_units, kBatchBlock, 0, stream>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(4)) != cudaSuccess) return e;
+        *launches += (bp.vert_units ? 1 : 0) + (bp.face_units ? 2 : 0) + (bp.tile_units ? 1 : 0);
+        return cudaSuccess;
+    }
     // resident CTAs per SM of this instantiation, per device (a cooperative launch must not
     // exceed it)
     constexpr int kMaxDev = 64;
     static int blocks_per_sm[kMaxDev] = {};
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
     if (blocks_per_sm[dev] == 0) {
         int n = 0;
@@ -412,8 +573,6 @@ cudaError_t launch_batch_s(const BatchParams& bp, int num_sms, cudaStream_t stre
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaMemsetAsync(bp.counters, 0, kBatchCountersReset, stream);
-    if (e != cudaSuccess) return e;
     if (bp.prof && (e = cudaMemsetAsync(&bp.prof->exits, 0, sizeof(bp.prof->exits), stream)) != cudaSuccess) return e;
     e = cudaLaunchKernelEx(&cfg, batch_kernel<S>, bp);
     if (e == cudaSuccess) *launches += 1;
@@ -422,13 +581,14 @@ cudaError_t launch_batch_s(const BatchParams& bp, int num_sms, cudaStream_t stre
 
 }  // namespace
 
-cudaError_t launch_batch(int shader, const BatchParams& bp, int num_sms, cudaStream_t stream, uint64_t* launches) {
+cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
+                         cudaEvent_t* phase_events, uint64_t* launches) {
     switch (shader) {
-        case kFlat: return launch_batch_s<kFlat>(bp, num_sms, stream, launches);
-        case kPhong: return launch_batch_s<kPhong>(bp, num_sms, stream, launches);
-        case kPBR: return launch_batch_s<kPBR>(bp, num_sms, stream, launches);
-        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, num_sms, stream, launches);
-        case kGouraud: return launch_batch_s<kGouraud>(bp, num_sms, stream, launches);
+        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, phase_events, launches);
+        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, phase_events, launches);
+        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, phase_events, launches);
+        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, phase_events, launches);
+        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches);
         default: return cudaErrorInvalidValue;
     }
 }

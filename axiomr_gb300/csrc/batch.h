@@ -7,10 +7,12 @@
 
 namespace axr {
 
-// Resets the work counters and grid-barrier words, then launches one cooperative grid of
-// (resident CTAs per SM) x num_sms CTAs running the four phases over the batch's draws,
-// which must all use shader kind `shader`. Adds the number of kernels launched to
-// *launches.
-cudaError_t launch_batch(int shader, const BatchParams& bp, int num_sms, cudaStream_t stream, uint64_t* launches);
+// Resets the work counters and grid-barrier words, then launches the batch's draws (all
+// of shader kind `shader`) in launch form `form`: kFormPersistent, one cooperative grid of
+// (resident CTAs per SM) x num_sms CTAs running the four phases; kFormPhased, four
+// launches. `phase_events` (optional, 5 events, phased form only) are recorded around the
+// four launches. Adds the number of kernels launched to *launches.
+cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
+                         cudaEvent_t* phase_events, uint64_t* launches);
 
 }  // namespace axr

@@ -127,13 +127,16 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     const uint32_t large_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(faces, 65536), 1u << 22);
     const uint32_t item_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(4 * faces, 1u << 20), 1u << 24);
     // work units of every draw (the same counts as the loop below assigns)
+    const int form = ctx->batch_form;
+    const uint32_t tiles_per_warp = form == kFormPersistent ? kPersistentTilesPerWarp : kPhasedTilesPerWarp;
+    const uint32_t tile_unit = kUnitWarps * tiles_per_warp;
     size_t total_units = 0;
     for (int32_t i = 0; i < count; ++i) {
         const axr_draw_desc& d = draws[i];
         const bool drawn = d.mesh->num_drawn > 0;
         total_units += (drawn ? ceil_div(d.mesh->num_vertices, kVertUnit) : 0u) + ceil_div(d.mesh->num_drawn, kFaceUnit);
         if (drawn || (d.clear_flags & (AXR_DRAW_CLEAR_COLOR | AXR_DRAW_CLEAR_DEPTH)))
-            total_units += ceil_div((uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y, kTileUnit);
+            total_units += ceil_div((uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y, tile_unit);
     }
     const size_t table_bytes = align256(sizeof(BatchDraw) * (size_t)std::max(count, 1));
     const size_t units_bytes = align256(sizeof(UnitRef) * std::max<size_t>(total_units, 1));
@@ -197,7 +200,7 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             const uint32_t nv = drawn ? ceil_div(m->num_vertices, kVertUnit) : 0u;
             const uint32_t nf = ceil_div(m->num_drawn, kFaceUnit);
             const uint32_t nt = (drawn || bd.flags & (kBatchClearColor | kBatchClearDepth))
-                                    ? ceil_div((uint64_t)fb->tiles_x * fb->tiles_y, kTileUnit)
+                                    ? ceil_div((uint64_t)fb->tiles_x * fb->tiles_y, tile_unit)
                                     : 0u;
             for (uint32_t j = 0; j < nv; ++j) uv.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nf; ++j) uf.push_back(UnitRef{(uint32_t)k, j});
@@ -222,6 +225,7 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         bp.tile_units = (uint32_t)ut.size();
         bp.large_cap = large_cap;
         bp.item_cap = item_cap;
+        bp.tiles_per_warp = tiles_per_warp;
         if (bp.vert_units + bp.face_units + bp.tile_units > 0) b->launches.push_back(L);
     }
     if (async) {
@@ -237,6 +241,7 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             AXR_CUDA(ctx, cudaMemcpy(d_units, units.data(), sizeof(UnitRef) * units.size(), cudaMemcpyHostToDevice));
     }
     b->device = ctx->device;
+    b->form = form;
     b->count = (uint32_t)count;
     b->vertices = verts;
     b->faces = faces;
@@ -249,8 +254,18 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
     for (const axr_batch::Launch& L : b->launches) {
         BatchParams bp = L.params;
         bp.collect_stats = ctx->collect_stats;
-        bp.prof = ctx->profile ? ctx->batch_prof : nullptr;
-        AXR_CUDA(ctx, launch_batch(L.shader, bp, ctx->cfg.num_sms, ctx->stream, &ctx->launches));
+        bp.prof = ctx->profile && b->form == kFormPersistent ? ctx->batch_prof : nullptr;
+        cudaEvent_t* ev = nullptr;
+        if (ctx->profile && b->form == kFormPhased && !ctx->capturing) {
+            while (ctx->batch_events.size() < ctx->batch_events_used + 5) {
+                cudaEvent_t e;
+                AXR_CUDA(ctx, cudaEventCreate(&e));
+                ctx->batch_events.push_back(e);
+            }
+            ev = &ctx->batch_events[ctx->batch_events_used];
+            ctx->batch_events_used += 5;
+        }
+        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, ctx->stream, ev, &ctx->launches));
     }
     return AXR_OK;
 }
@@ -258,6 +273,12 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
 }  // namespace
 
 namespace axr_internal {
+
+axr_status batch_plan(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch* b, bool async) {
+    return plan_batch(ctx, draws, count, b, async);
+}
+
+axr_status batch_launch(axr_context* ctx, const axr_batch* b) { return launch_planned(ctx, b); }
 
 void encode_framebuffer_maps(axr_framebuffer* fb) {
     fb->tma = false;
@@ -350,6 +371,7 @@ axr_status axr_batch_get_info(const axr_batch* b, axr_batch_info* out) {
     if (!b || !out) return fail(nullptr, AXR_E_INVALID, "NULL argument");
     out->draws = b->count;
     out->launches = (uint32_t)b->launches.size();
+    out->form = b->form;
     out->vertices = b->vertices;
     out->faces = b->faces;
     out->pixels = b->pixels;
@@ -404,6 +426,34 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
     AXR_CUDA(ctx, cudaEventCreate(&e1));
     axr_batch trial;
     st = AXR_OK;
+    // time `sub` as planned now: warm-up launch, then `repeats` launches between events
+    auto time_plan = [&](const axr_draw_desc* sub, int32_t n, float* ms) -> axr_status {
+        axr_status r = plan_batch(ctx, sub, n, &trial, false);
+        if (r != AXR_OK) return r;
+        if ((r = launch_planned(ctx, &trial)) != AXR_OK) return r;
+        cudaError_t e = cudaEventRecord(e0, ctx->stream);
+        for (int32_t i = 0; i < repeats && e == cudaSuccess && r == AXR_OK; ++i) r = launch_planned(ctx, &trial);
+        if (r != AXR_OK) return r;
+        if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        return e == cudaSuccess ? AXR_OK : cuda_fail(ctx, e, "autotune timing");
+    };
+    // launch form: both forms on the whole batch
+    {
+        float best_ms = 0.f;
+        int best = ctx->batch_form;
+        for (int form : {kFormPersistent, kFormPhased}) {
+            ctx->batch_form = form;
+            float ms = 0.f;
+            if ((st = time_plan(draws, count, &ms)) != AXR_OK) break;
+            if (best_ms == 0.f || ms < best_ms) {
+                best_ms = ms;
+                best = form;
+            }
+        }
+        ctx->batch_form = best;
+    }
     for (int k = 0; k < AXR_TUNE_CLASSES && st == AXR_OK; ++k) {
         const std::vector<axr_draw_desc>& sub = by_class[(size_t)k];
         if (sub.empty()) continue;
@@ -411,17 +461,8 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
         int32_t best = ctx->tune_small[k];
         for (int32_t cand : kCandidates) {
             ctx->tune_small[k] = cand;
-            st = plan_batch(ctx, sub.data(), (int32_t)sub.size(), &trial, false);
-            if (st != AXR_OK) break;
-            if ((st = launch_planned(ctx, &trial)) != AXR_OK) break;  // warm-up
-            cudaError_t e = cudaEventRecord(e0, ctx->stream);
-            for (int32_t r = 0; r < repeats && e == cudaSuccess && st == AXR_OK; ++r) st = launch_planned(ctx, &trial);
-            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
-            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            if (e != cudaSuccess) st = cuda_fail(ctx, e, "autotune timing");
-            if (st != AXR_OK) break;
+            if ((st = time_plan(sub.data(), (int32_t)sub.size(), &ms)) != AXR_OK) break;
             if (best_ms == 0.f || ms < best_ms) {
                 best_ms = ms;
                 best = cand;
@@ -437,5 +478,16 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
     if (out_small_max_pixels) std::memcpy(out_small_max_pixels, ctx->tune_small, sizeof(ctx->tune_small));
     return AXR_OK;
 }
+
+axr_status axr_batch_set_form(axr_context* ctx, int32_t form) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    if (form != AXR_BATCH_PERSISTENT && form != AXR_BATCH_PHASED)
+        return fail(ctx, AXR_E_INVALID, "unknown batch launch form %d", form);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->batch_form = form;
+    return AXR_OK;
+}
+
+int32_t axr_batch_get_form(const axr_context* ctx) { return ctx ? ctx->batch_form : -1; }
 
 }  // extern "C"

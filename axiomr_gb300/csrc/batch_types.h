@@ -10,8 +10,8 @@
 //   vertex caches         per draw: vscreen[V] float4 + vattr[n*V] float4 (n = VAttr<S>::n)
 //   LargeTri[large_cap], large_draw[large_cap], LargeItem[item_cap]: shared by all draws
 // Work units: 256 vertices (vertex phase), 256 faces in draw order (geometry phase),
-// 64 tiles of 16x16, 8 per warp (key-scan + shade phase); the large-triangle phase takes
-// items from the shared list.
+// 8 x tiles_per_warp tiles of 16x16 (key-scan + shade phase); the large-triangle phase
+// takes items from the shared list.
 #pragma once
 #include <stdint.h>
 
@@ -30,8 +30,7 @@ constexpr uint32_t kBatchTma = 4u;         // the tensor maps are valid (width %
 
 constexpr uint32_t kVertUnit = 256;
 constexpr uint32_t kFaceUnit = 256;
-constexpr uint32_t kTileUnit = 64;
-constexpr uint32_t kTilesPerWarp = 8;
+constexpr uint32_t kUnitWarps = 8;  // warps of a 256-thread CTA
 
 struct alignas(64) BatchDraw {
     TensorMap128 color_map;  // uint32 [height][width], 16x16 box
@@ -75,7 +74,15 @@ struct BatchParams {
     uint32_t vert_units, face_units, tile_units;
     uint32_t large_cap, item_cap;
     int32_t collect_stats;
-    int32_t pad_;
+    uint32_t tiles_per_warp;      // tiles a warp takes per tile unit (unit = 8 warps x this)
 };
+
+// Launch forms of a batch (chosen per batch by the autotuner):
+//   kFormPersistent  one cooperative launch: the four phases behind grid barriers
+//   kFormPhased      four launches (one per phase), each over the work units of all draws
+constexpr int kFormPersistent = 0;
+constexpr int kFormPhased = 1;
+constexpr uint32_t kPersistentTilesPerWarp = 8;
+constexpr uint32_t kPhasedTilesPerWarp = 1;
 
 }  // namespace axr

@@ -53,6 +53,9 @@ WORKLOADS = {
                               "triangles), resolution uniform from {256^2, 512^2, 1024^2, 1920x1080}, camera on a "
                               "random orbit at distance 2-6, one of 8 1024^2 RGBA8 noise textures, Blinn-Phong"),
 }
+WORKLOADS["serve"] = (None, "open-loop Poisson arrivals; 90% requests of the small-triangle configuration (200,000 "
+                            "triangles, 3840x2160, Gouraud; one of 64 seeded soups), 10% heightfields (2,093,058 "
+                            "triangles, 1920x1080, Blinn-Phong, random camera azimuth); 40 GB residency budget")
 BATCH_REF_SAMPLE = 16  # draws of the mixed batch the CPU arms render per step (every 32nd)
 L2_FLUSH_BYTES = 256 << 20
 
@@ -67,6 +70,11 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true", help="batch: plan with the default tuning table")
     ap.add_argument("--draws", type=int, default=512, help="batch: number of draws (a smaller batch for profiling)")
     ap.add_argument("--scale", type=float, default=1.0, help="batch: framebuffer size scale (profiling)")
+    ap.add_argument("--rates", default="100,500,2000,5000", help="serve: offered loads, requests/s")
+    ap.add_argument("--serve-seconds", type=float, default=30.0, help="serve: duration of each offered load")
+    ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: device-memory residency budget")
+    ap.add_argument("--readback", choices=("colour", "none"), default="colour",
+                    help="serve: read each request's colour plane back to host memory, or not")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -463,6 +471,26 @@ def batch_algo_bytes(scenes, frags: float) -> float:
     return b
 
 
+def batch_phase_bytes(scenes, frags: float, tiles: int) -> dict:
+    """Algorithmic bytes of each phase of one batched step (Blinn-Phong: 48-byte vertex
+    cache entries): vertices read (32) + cache written (48) per vertex; indices (12 per
+    face) + cache gathers (16 per vertex) + one key per covered fragment (8) for the face
+    and large phases together; the tile pass writes colour + depth once per pixel (8),
+    reads the flags (4 per tile), reads and resets the key of every covered pixel (16),
+    reads the vertex cache (48 per vertex) and min(texture, 4 per covered fragment)."""
+    total_faces = sum(int(sc.mesh.indices.shape[0]) for sc in scenes)
+    v = f = px = tex = 0.0
+    for sc in scenes:
+        V, F = sc.mesh.positions.shape[0], sc.mesh.indices.shape[0]
+        t = sum(int(m.diffuse.nbytes) for m in sc.mesh.materials if m.diffuse is not None)
+        v += V
+        f += F
+        px += sc.width * sc.height
+        tex += min(t, 4.0 * frags * F / max(1, total_faces))
+    return {"vertex": 80.0 * v, "face": 12.0 * f + 16.0 * v + 8.0 * frags, "large": 8.0 * frags,
+            "tile": 8.0 * px + 4.0 * tiles + 16.0 * frags + 48.0 * v + tex}
+
+
 def run_batch(args, dist: Dist):
     """The mixed batch: 512 draws into 512 framebuffers per step, batched form (one
     persistent launch, replayed from a CUDA graph) against the plain per-draw path (clear,
@@ -576,12 +604,27 @@ def run_batch(args, dist: Dist):
     for p in keep:
         lib.axr_host_free(p)
 
+    # per-phase device time of one batch (eager launches with profiling on)
+    ctx.profile(True)
+    ctx.profile()
+    for _ in range(3):
+        batch.launch()
+    pr = ctx.profile()
+    ctx.profile(False)
+    nl = max(1, pr["batch_launches"])
+    phase_ms = {k: pr[f"batch_{k}_ms"] / nl for k in ("vertex", "face", "large", "tile")}
+
     hbm_peak, peak_kind = measured_peaks()
     ms = total_ms / len(step_ms)
     frags = float(st["fragments"])
     algo = batch_algo_bytes(scenes, frags)
     achieved = algo / (ms * 1e-3) / 1e9
     faces = info["faces"]
+    pb = batch_phase_bytes(scenes, frags, int(info["tiles"]))
+    dom = max(phase_ms, key=phase_ms.get)
+    kernel_of = {"vertex": "batch_vertex_kernel", "face": "batch_face_kernel", "large": "batch_large_kernel",
+                 "tile": "batch_tile_kernel"} if info["form"] == 1 else {k: "batch_kernel" for k in phase_ms}
+    dom_achieved = pb[dom] / (phase_ms[dom] * 1e-3) / 1e9 if phase_ms[dom] > 0 else 0.0
     out = {
         "metric": "frames/s", "value": round(value, 2), "unit": "frames/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -608,10 +651,16 @@ def run_batch(args, dist: Dist):
                         "framebuffers into pinned memory; meshes and textures resident",
                 "gpu_launches_per_step": e2e_launches},
         "gpu_launches": int(info["launches"]) * len(step_ms),
-        "roofline": {"bound": "hbm", "kernel": "batch_kernel", "achieved": round(achieved, 1), "peak": hbm_peak,
-                     "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                     "traffic": profiled_traffic("batch_kernel", "batch"), "algorithmic_bytes": algo,
-                     "launch_us": round(ms * 1e3, 2)},
+        "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),
+                     "peak": hbm_peak, "peak_source": peak_kind, "unit": "GB/s",
+                     "frac": round(dom_achieved / hbm_peak, 4), "traffic": profiled_traffic(kernel_of[dom], "batch"),
+                     "algorithmic_bytes": pb[dom], "launch_us": round(phase_ms[dom] * 1e3, 2),
+                     "phase_us": {k: round(v * 1e3, 2) for k, v in phase_ms.items()}},
+        "frame_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                           "frac": round(achieved / hbm_peak, 4), "algorithmic_bytes": algo,
+                           "definition": "per draw V*32 + F*12 + W*H*8 + min(texture, 4 per covered fragment), "
+                                         "over the whole step"},
+        "form": "phased" if info["form"] == 1 else "persistent",
         "clocks": sampler.summary(),
     }
     graph.close()
@@ -619,6 +668,102 @@ def run_batch(args, dist: Dist):
     batch.close()
     ctx.close()
     return out, scenes
+
+
+def run_serve(args, dist: Dist):
+    """Serving loop under open-loop Poisson load: per offered rate, p50/p99 latency (arrival
+    to colour read-back done, server clock) and achieved frames/s, for the batched loop and
+    for the same loop rendering every request alone with the per-draw path."""
+    from axiomr_gb300 import api
+
+    desc = WORKLOADS["serve"][1]
+    rng = np.random.default_rng(6)
+    soups = [W.soup_scene(seed=1000 + k) for k in range(64)]
+    hf = W.heightfield_scene()
+    rates = [float(r) for r in args.rates.split(",") if r]
+    cam_soup = api.Camera.from_workload(soups[0].camera)
+    gouraud, blinn = api.GouraudShader(), api.BlinnPhongShader()
+    out_modes = {}
+    for mode in ("batched", "per_request"):
+        srv = api.Server(dist.local_rank, budget_bytes=int(args.budget_gb * (1 << 30)), max_batch=64, max_inflight=2,
+                         per_request=(mode == "per_request"))
+        soup_ids = [srv.add_mesh(sc.mesh) for sc in soups]
+        hf_id = srv.add_mesh(hf.mesh)
+        # pinned colour buffers, reused round robin by the requests in flight
+        ring = []
+        keep = []
+        lib = srv.lib
+        if args.readback == "colour":
+            ring = [pinned_like(lib, np.zeros((2160, 3840, 4), np.uint8), keep) for _ in range(96)]
+            hf_ring = [pinned_like(lib, np.zeros((1080, 1920, 4), np.uint8), keep) for _ in range(16)]
+        else:
+            ring, hf_ring = [None], [None]
+        # warm-up: every asset resident once, framebuffer pools filled
+        ts = [srv.submit(i, cam_soup, gouraud, 3840, 2160, out_bgra=ring[k % len(ring)]) for k, i in enumerate(soup_ids)]
+        ts.append(srv.submit(hf_id, api.Camera.from_workload(hf.camera), blinn, 1920, 1080, out_bgra=hf_ring[0]))
+        for t in ts:
+            srv.wait(t)
+        per_rate = []
+        for rate in rates:
+            n = max(1, int(rate * args.serve_seconds))
+            gaps = rng.exponential(1.0 / rate, n)
+            offs = (np.cumsum(gaps) * 1e9).astype(np.int64)
+            kinds = rng.random(n) < 0.9
+            which = rng.integers(0, len(soup_ids), n)
+            az = rng.random(n) * 360.0
+            tickets = [None] * n
+            t0 = srv.now_ns() + 2_000_000
+            k = 0
+            soup_slot = hf_slot = 0
+            while k < n:
+                now = srv.now_ns()
+                while k < n and t0 + int(offs[k]) <= now:
+                    if kinds[k]:
+                        tickets[k] = srv.submit(soup_ids[which[k]], cam_soup, gouraud, 3840, 2160,
+                                                out_bgra=ring[soup_slot % len(ring)], arrival_ns=t0 + int(offs[k]))
+                        soup_slot += 1
+                    else:
+                        c = W.orbit_camera(2.5, 30.0, float(az[k]), 1920, 1080)
+                        tickets[k] = srv.submit(hf_id, api.Camera.from_workload(c), blinn, 1920, 1080,
+                                                out_bgra=hf_ring[hf_slot % len(hf_ring)], arrival_ns=t0 + int(offs[k]))
+                        hf_slot += 1
+                    k += 1
+                if k < n:
+                    wait = (t0 + int(offs[k]) - srv.now_ns()) / 1e9
+                    if wait > 2e-4:
+                        time.sleep(wait - 1e-4)
+            lat, sizes, first, last, fails = [], [], None, 0, 0
+            for t in tickets:
+                r = srv.wait(t)
+                if r["status"] != 0:
+                    fails += 1
+                    continue
+                lat.append((r["done_ns"] - r["arrival_ns"]) / 1e6)
+                sizes.append(r["batch_size"])
+                last = max(last, r["done_ns"])
+            span = (last - t0) / 1e9
+            lat = np.asarray(lat)
+            per_rate.append({"offered_rps": rate, "requests": n, "failed": fails,
+                             "achieved_fps": round(len(lat) / span, 1) if span > 0 else None,
+                             "p50_ms": round(float(np.percentile(lat, 50)), 3) if lat.size else None,
+                             "p99_ms": round(float(np.percentile(lat, 99)), 3) if lat.size else None,
+                             "mean_batch": round(float(np.mean(sizes)), 2) if sizes else None})
+            print(json.dumps({"mode": mode, **per_rate[-1]}), file=sys.stderr, flush=True)
+        st = srv.stats()
+        srv.close()
+        for p in keep:
+            lib.axr_host_free(p)
+        out_modes[mode] = {"rates": per_rate, "uploads": st["uploads"], "evictions": st["evictions"],
+                           "framebuffers": st["framebuffers"], "peak_resident_gb": round(st["peak_bytes"] / 2**30, 2)}
+    top = out_modes["batched"]["rates"][-1]
+    return {
+        "metric": "frames/s", "value": top["achieved_fps"], "unit": "frames/s", "n_gpus": dist.world,
+        "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
+        "config": {"workload": f"serve: {desc}", "seconds_per_rate": args.serve_seconds, "max_batch": 64,
+                   "max_inflight": 2, "budget_gb": args.budget_gb, "readback": args.readback},
+        "serving": out_modes,
+    }
 
 
 def cpu_batch_sample(scenes, budget_s: float, steps: int):
@@ -667,7 +812,7 @@ def run_reference(args, dist: Dist):
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
-    scene = make()
+    scene = make() if make is not None else W.soup_scene(seed=1000)  # serve: one request of the common kind
     from oracle import Oracle
 
     port = Oracle("port")
@@ -716,6 +861,11 @@ def main():
         if args.impl == "reference":
             if dist.rank == 0:
                 print(json.dumps(run_reference(args, dist)), flush=True)
+            return
+        if args.workload == "serve":
+            out = run_serve(args, dist)
+            if dist.rank == 0:
+                print(json.dumps(out), flush=True)
             return
         if args.workload == "batch":
             out, scenes = run_batch(args, dist)

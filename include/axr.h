@@ -228,14 +228,25 @@ typedef struct axr_batch axr_batch;
  * the upload. Meshes, framebuffers and textures must outlive the batch. */
 axr_status axr_batch_create(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch** out);
 /* Enqueue the planned batch on the context stream (per shader kind: a counter reset and
- * one cooperative launch). Allocates nothing and reads no host memory, so it can be
+ * the launches of its form). Allocates nothing and reads no host memory, so it can be
  * recorded into a CUDA graph (axr_graph_begin / axr_graph_end) and replayed. */
 axr_status axr_batch_launch(axr_context* ctx, axr_batch* batch);
 void axr_batch_destroy(axr_context* ctx, axr_batch* batch);
 
+/* Launch forms (the autotuner picks one per batch; batches planned afterwards use it):
+ * PERSISTENT: one cooperative launch per shader kind, its four phases (vertices, faces,
+ * large-triangle tiles, tile pass) behind grid barriers; PHASED: four launches per shader
+ * kind, one per phase, each over the work units of every draw. */
+#define AXR_BATCH_PERSISTENT 0
+#define AXR_BATCH_PHASED 1
+axr_status axr_batch_set_form(axr_context* ctx, int32_t form);
+int32_t axr_batch_get_form(const axr_context* ctx);
+
 typedef struct axr_batch_info {
     uint32_t draws;
-    uint32_t launches;        /* cooperative launches per axr_batch_launch (shader kinds) */
+    uint32_t launches;        /* shader-kind groups (each one launch set) per axr_batch_launch */
+    int32_t form;             /* AXR_BATCH_* the batch was planned for */
+    uint32_t pad_;
     uint64_t vertices;        /* vertices of all draws */
     uint64_t faces;           /* faces in draw order of all draws */
     uint64_t pixels;          /* framebuffer pixels of all draws */
@@ -248,13 +259,14 @@ axr_status axr_batch_get_info(const axr_batch* batch, axr_batch_info* out);
  * and launch it. Not for graph capture (the draw table is uploaded by this call). */
 axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count);
 
-/* Autotuner. A draw's density class is the estimated mean screen area of its front-facing
- * triangles, from the mesh's bounding sphere projected through its camera: class k covers
- * [2^(2k-1), 2^(2k+1)) pixels (class 0 below 2, the last class 512 and above). Per class
- * the tuner picks the largest triangle pixel box rasterised by one thread (larger boxes
- * go to the warp-per-tile rasteriser) by timing sub-batches of the given draws' classes
- * with each candidate `repeats` times. The table is the context's; batches planned
- * afterwards use it. out_small_max_pixels (optional) receives the table. */
+/* Autotuner. First the launch form, timing the whole batch in both forms. Then, per
+ * density class, the largest triangle pixel box rasterised by one thread (larger boxes go
+ * to the warp-per-tile rasteriser), timing the sub-batch of the given draws in that class
+ * with each candidate `repeats` times. A draw's density class is the estimated mean screen
+ * area of its front-facing triangles, from the mesh's bounding sphere projected through
+ * its camera: class k covers [2^(2k-1), 2^(2k+1)) pixels (class 0 below 2, the last class
+ * 512 and above). The form and the table are the context's; batches planned afterwards
+ * use them. out_small_max_pixels (optional) receives the table. */
 #define AXR_TUNE_CLASSES 6
 axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int32_t count, int32_t repeats,
                               int32_t out_small_max_pixels[AXR_TUNE_CLASSES]);
@@ -262,6 +274,103 @@ axr_status axr_batch_get_tuning(const axr_context* ctx, int32_t small_max_pixels
 axr_status axr_batch_set_tuning(axr_context* ctx, const int32_t small_max_pixels[AXR_TUNE_CLASSES]);
 /* Density class of one draw (the classification the planner uses). */
 int32_t axr_draw_density_class(const axr_draw_desc* draw);
+
+/* ------------------------------------------------------------------ serving loop
+ * No reference counterpart (the reference renders frames in its application loop,
+ * src/renderer.cpp:98-130). A server owns a context on one device and a host thread that
+ * runs a continuous-batching render loop: requests (mesh asset, camera, model, shader,
+ * resolution, clears) are admitted as device memory and batch slots free up, each
+ * admitted group is rendered as one batch (axr_batch_* machinery) while the previous
+ * group's read-backs are in flight, and results (BGRA colour and/or depth) are copied to
+ * the request's host buffers. Mesh assets and textures are registered once with host
+ * copies; the server keeps them resident on the device and evicts the least recently
+ * used ones (not pinned by in-flight requests) when the device-memory budget for resident
+ * meshes, textures and framebuffers would be exceeded (the loop's batch scratch and
+ * per-draw scratch are its working memory, outside the budget). Framebuffers are pooled
+ * per resolution. Latency is measured on the server's clock (axr_server_now_ns). */
+typedef struct axr_server axr_server;
+
+typedef struct axr_server_config {
+    int32_t device;
+    uint64_t memory_budget_bytes; /* device memory for resident meshes, textures, framebuffers */
+    int32_t max_batch;            /* requests per batch (continuous-batching cap) */
+    int32_t max_inflight;         /* batches on the GPU at once (their read-backs overlap) */
+    int32_t per_request;          /* 1: render each request alone with the per-draw path
+                                     (clearColor, clearDepth, drawMesh), no batching */
+    int32_t pad_;
+} axr_server_config;
+
+/* A texture asset (RGBA8, row 0 first); *out_id receives its id. */
+axr_status axr_server_add_texture(axr_server* srv, const uint8_t* rgba, int32_t width, int32_t height,
+                                  int32_t* out_id);
+/* A mesh asset: arrays as in axr_mesh_desc, materials naming texture asset ids (-1: none);
+ * the server keeps host copies. *out_id receives its id. */
+typedef struct axr_server_material {
+    int32_t diffuse, bump, metallic, roughness, ao; /* texture asset ids or -1 */
+    float specular_exponent;
+} axr_server_material;
+typedef struct axr_server_mesh_desc {
+    uint32_t num_vertices;
+    const float* positions;
+    const float* uvs;
+    const float* normals;
+    const float* tangents;   /* or NULL */
+    const float* bitangents; /* or NULL */
+    uint32_t num_faces;
+    const uint32_t* indices;
+    uint32_t num_groups;
+    const axr_group_desc* groups;
+    uint32_t num_materials;
+    const axr_server_material* materials;
+} axr_server_mesh_desc;
+axr_status axr_server_add_mesh(axr_server* srv, const axr_server_mesh_desc* desc, int32_t* out_id);
+
+typedef struct axr_server_request {
+    int32_t mesh;             /* mesh asset id */
+    int32_t width, height;    /* framebuffer resolution */
+    float model[16];
+    axr_camera_desc camera;
+    axr_shader_desc shader;
+    uint32_t clear_flags;     /* AXR_DRAW_CLEAR_* */
+    uint8_t clear_rgba[4];
+    float clear_depth;
+    uint64_t arrival_ns;      /* arrival time on the server clock (0: the submit time) */
+    uint8_t* out_bgra;        /* host destination of the colour plane (W*H*4), or NULL */
+    float* out_depth;         /* host destination of the depth plane (W*H), or NULL */
+} axr_server_request;
+
+typedef struct axr_server_result {
+    int32_t status;           /* axr_status of the request */
+    uint32_t batch_size;      /* requests rendered in the same batch */
+    uint64_t arrival_ns;      /* server clock */
+    uint64_t launch_ns;       /* its batch was launched */
+    uint64_t done_ns;         /* its read-back finished */
+    uint64_t batch_id;
+} axr_server_result;
+
+typedef struct axr_server_stats {
+    uint64_t submitted, completed, batches;
+    uint64_t uploads;         /* assets made resident (meshes and textures) */
+    uint64_t evictions;       /* assets evicted to fit the budget */
+    uint64_t framebuffers;    /* framebuffers allocated */
+    uint64_t resident_bytes;  /* device memory held now */
+    uint64_t peak_bytes;
+} axr_server_stats;
+
+axr_status axr_server_create(const axr_server_config* cfg, axr_server** out);
+/* Stops the loop after the queued requests are done, then frees everything. */
+void axr_server_destroy(axr_server* srv);
+uint64_t axr_server_now_ns(void);
+/* Queue a request; *ticket identifies it. Host buffers must stay valid until it is done. */
+axr_status axr_server_submit(axr_server* srv, const axr_server_request* req, uint64_t* ticket);
+/* Wait up to timeout_ms (negative: no limit) for a request; AXR_E_TIMEOUT if not done. */
+axr_status axr_server_wait(axr_server* srv, uint64_t ticket, int32_t timeout_ms, axr_server_result* out);
+axr_status axr_server_get_stats(axr_server* srv, axr_server_stats* out);
+/* hold != 0: admit nothing (requests queue up; the batches in flight finish); hold == 0:
+ * resume, admitting the queue as batches. For draining a node or grouping a burst. */
+axr_status axr_server_hold(axr_server* srv, int32_t hold);
+/* Message of the server's last failure ("" if none). */
+const char* axr_server_last_error(axr_server* srv);
 
 /* ------------------------------------------------------------------ CUDA graphs
  * Record the draws issued on the context between begin and end into a CUDA graph and

@@ -1,0 +1,127 @@
+"""Serving loop (axr_server_*): results are the same rendered alone and in a mix of
+concurrent requests (exactly: the same device functions compute every value), equal to
+the per-draw path and within the parity bar of the oracle; assets are evicted and
+re-uploaded under a small device-memory budget without changing results; per-request
+mode gives the same frames; oversized requests and bad arguments are rejected."""
+import numpy as np
+import pytest
+
+from axiomr_gb300 import api
+from axiomr_gb300 import workloads as W
+from axiomr_gb300._lib import AXR_OK, AxrError
+from helpers import assert_parity
+
+pytestmark = pytest.mark.gpu
+
+
+def scenes_mix():
+    out = []
+    for k in range(4):
+        out.append(W.soup_scene(count=3000, width=160 + 8 * k, height=120, seed=40 + k, edge_min=1, edge_max=12,
+                                depth_min=0.2, depth_max=50.0))
+    for k, (w, h, lon) in enumerate(((128, 128, 32), (200, 100, 16), (96, 160, 48))):
+        sc = W.sphere_scene(width=w, height=h, lon=lon, lat=lon // 2, tex_size=64, tex_seed=7 + k)
+        out.append(sc)
+    return out
+
+
+def request(srv, ids, sc, k):
+    bgra = np.zeros((sc.height, sc.width, 4), np.uint8)
+    depth = np.zeros((sc.height, sc.width), np.float32)
+    sh = sc.shader
+    b, g, r, a = sc.clear_bgra
+    t = srv.submit(ids[k], api.Camera.from_workload(sc.camera), api.Shader(sh.kind, tuple(sh.light_direction),
+                   tuple(sh.light_color)), sc.width, sc.height, sc.model, (r, g, b, a), float("inf"), bgra, depth)
+    return t, bgra, depth
+
+
+def per_draw(ctx, sc):
+    return api.render_scene(ctx, sc)
+
+
+def test_same_alone_and_in_mix(ctx, port):
+    scenes = scenes_mix()
+    srv = api.Server(0, budget_bytes=2 << 30, max_batch=8, max_inflight=2)
+    ids = [srv.add_mesh(sc.mesh) for sc in scenes]
+    # alone
+    alone = []
+    for k, sc in enumerate(scenes):
+        t, bgra, depth = request(srv, ids, sc, k)
+        res = srv.wait(t, 60000)
+        assert res["status"] == AXR_OK and res["batch_size"] == 1
+        alone.append((bgra, depth))
+    # in a mix: every scene three times, queued while the loop holds, then released
+    order = [k % len(scenes) for k in range(3 * len(scenes))]
+    srv.hold(True)
+    pending = [(k,) + request(srv, ids, scenes[k], k) for k in order]
+    srv.hold(False)
+    sizes = []
+    for k, t, bgra, depth in pending:
+        res = srv.wait(t, 60000)
+        assert res["status"] == AXR_OK
+        sizes.append(res["batch_size"])
+        assert np.array_equal(bgra, alone[k][0]) and np.array_equal(depth.view(np.uint32), alone[k][1].view(np.uint32)), \
+            f"scene {k} differs between alone and mixed (batch of {res['batch_size']})"
+    assert max(sizes) > 1, "the mix was never batched"
+    st = srv.stats()
+    assert st["completed"] == len(scenes) + len(order) and st["batches"] < st["completed"]
+    assert max(sizes) == 8  # max_batch
+    srv.close()
+    # equal to the per-draw path, and to the oracle within the parity bar
+    for k, sc in enumerate(scenes):
+        got = per_draw(ctx, sc)
+        assert np.array_equal(got[0], alone[k][0]) and np.array_equal(got[1].view(np.uint32), alone[k][1].view(np.uint32))
+        if k % 3 == 0:
+            assert_parity(alone[k], port.draw(sc, port.camera(sc.camera)[2]), f"served scene {k} vs oracle")
+
+
+def test_eviction_under_small_budget(ctx):
+    scenes = scenes_mix()
+    # room for about two framebuffers and a few meshes: assets must come and go
+    srv = api.Server(0, budget_bytes=3 << 20, max_batch=4, max_inflight=2)
+    ids = [srv.add_mesh(sc.mesh) for sc in scenes]
+    expect = [per_draw(ctx, sc) for sc in scenes]
+    pending = []
+    for rep in range(3):
+        for k, sc in enumerate(scenes):
+            pending.append((k,) + request(srv, ids, sc, k))
+    for k, t, bgra, depth in pending:
+        res = srv.wait(t, 60000)
+        assert res["status"] == AXR_OK, res
+        assert np.array_equal(bgra, expect[k][0]) and np.array_equal(depth.view(np.uint32), expect[k][1].view(np.uint32))
+    st = srv.stats()
+    assert st["evictions"] > 0 and st["uploads"] > len(scenes)
+    assert st["peak_bytes"] <= 3 << 20
+    srv.close()
+
+
+def test_per_request_mode_matches(ctx):
+    scenes = scenes_mix()[:4]
+    srv = api.Server(0, budget_bytes=1 << 30, max_batch=8, max_inflight=2, per_request=True)
+    ids = [srv.add_mesh(sc.mesh) for sc in scenes]
+    pending = [(k,) + request(srv, ids, sc, k) for k, sc in enumerate(scenes)]
+    for k, t, bgra, depth in pending:
+        res = srv.wait(t, 60000)
+        assert res["status"] == AXR_OK
+        exp = per_draw(ctx, scenes[k])
+        assert np.array_equal(bgra, exp[0]) and np.array_equal(depth.view(np.uint32), exp[1].view(np.uint32))
+    srv.close()
+
+
+def test_oversized_request_and_bad_arguments():
+    sc = W.sphere_scene(width=64, height=64, lon=8, lat=4, tex_size=8)
+    srv = api.Server(0, budget_bytes=1 << 20, max_batch=4, max_inflight=1)
+    mid = srv.add_mesh(sc.mesh)
+    cam = api.Camera.from_workload(sc.camera)
+    t = srv.submit(mid, cam, api.BlinnPhongShader(), 4096, 4096)  # 4096^2 framebuffer > 1 MiB
+    res = srv.wait(t, 60000)
+    assert res["status"] == 3  # AXR_E_BUDGET
+    t = srv.submit(mid, cam, api.BlinnPhongShader(), 64, 64)
+    assert srv.wait(t, 60000)["status"] == AXR_OK
+    with pytest.raises(AxrError):
+        srv.submit(mid + 5, cam, api.BlinnPhongShader(), 64, 64)
+    with pytest.raises(AxrError):
+        srv.submit(mid, cam, api.Shader(9), 64, 64)
+    with pytest.raises(AxrError):
+        srv.wait(123456, 10)
+    srv.close()
