@@ -76,7 +76,8 @@ class Profile(C.Structure):
 
 
 class DrawStats(C.Structure):
-    _fields_ = [("triangles", C.c_uint64), ("fragments", C.c_uint64), ("large", C.c_uint64), ("tiles", C.c_uint64)]
+    _fields_ = [("triangles", C.c_uint64), ("fragments", C.c_uint64), ("large", C.c_uint64), ("tiles", C.c_uint64),
+                ("tested", C.c_uint64), ("shaded", C.c_uint64)]
 
 
 class ServerConfig(C.Structure):
@@ -161,6 +162,7 @@ SIGNATURES = {
     "axr_batch_set_tuning": (S, [P, P]),
     "axr_draw_density_class": (C.c_int32, [P]),
     "axr_batch_set_form": (S, [P, C.c_int32]),
+    "axr_measure_fp32_peak": (S, [P, C.POINTER(C.c_double)]),
     "axr_server_create": (S, [P, PP]),
     "axr_server_destroy": (None, [P]),
     "axr_server_now_ns": (C.c_uint64, []),

@@ -63,7 +63,8 @@ class Context:
             return None
         s = DrawStats()
         check(self.lib.axr_stats_read(self.handle, C.byref(s)), self.handle)
-        return {"triangles": s.triangles, "fragments": s.fragments, "large": s.large, "tiles": s.tiles}
+        return {"triangles": s.triangles, "fragments": s.fragments, "large": s.large, "tiles": s.tiles,
+                "tested": s.tested, "shaded": s.shaded}
 
     def profile(self, enable: Optional[bool] = None):
         """Enable/disable stage timing, or (no argument) read and reset it."""
@@ -78,6 +79,12 @@ class Context:
                 "batch_launches": pr.batch_launches, "batch_vertex_ms": pr.batch_vertex_ms,
                 "batch_face_ms": pr.batch_face_ms, "batch_large_ms": pr.batch_large_ms,
                 "batch_tile_ms": pr.batch_tile_ms}
+
+    def fp32_peak_tflops(self) -> float:
+        """FP32 issue peak of the device, measured with independent FMA chains."""
+        out = C.c_double()
+        check(self.lib.axr_measure_fp32_peak(self.handle, C.byref(out)), self.handle)
+        return out.value
 
     def tuning(self) -> list:
         """The batched form's tuning table: per density class, the largest triangle pixel

@@ -74,11 +74,13 @@ void free_scratch(axr_context* ctx) {
     dfree(ctx->vattr);
     dfree(ctx->shade);
     dfree(ctx->clip_px);
+    dfree(ctx->rec);
     ctx->large = nullptr;
     ctx->items = nullptr;
     ctx->vscreen = ctx->vattr = nullptr;
     ctx->shade = ctx->clip_px = nullptr;
-    ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->px_cap = 0;
+    ctx->rec = nullptr;
+    ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->px_cap = ctx->rec_cap = 0;
 }
 
 axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uint64_t pixels) {
@@ -90,8 +92,9 @@ axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uin
     uint32_t want_items = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1u << 20, 4ull * faces), 1u << 27);
     uint32_t want_verts = std::max<uint32_t>(4096, vertices);
     uint32_t want_px = (uint32_t)std::max<uint64_t>(1u << 16, pixels);
+    uint32_t want_rec = std::max<uint32_t>(4096, faces);  // one shading record per face
     if (want_tris <= ctx->large_cap && want_items <= ctx->item_cap && want_verts <= ctx->vcap &&
-        want_px <= ctx->px_cap)
+        want_px <= ctx->px_cap && want_rec <= ctx->rec_cap)
         return AXR_OK;
     if (ctx->capturing)
         return fail(ctx, AXR_E_CAPACITY, "scratch for %u faces / %u vertices not reserved before graph capture",
@@ -100,6 +103,7 @@ axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uin
     want_items = std::max(want_items, ctx->item_cap);
     want_verts = std::max(want_verts, ctx->vcap);
     want_px = std::max(want_px, ctx->px_cap);
+    want_rec = std::max(want_rec, ctx->rec_cap);
     AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     free_scratch(ctx);
     AXR_CUDA(ctx, dmalloc(&ctx->large, want_tris));
@@ -108,6 +112,8 @@ axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uin
     AXR_CUDA(ctx, dmalloc(&ctx->vattr, 4ull * want_verts));
     AXR_CUDA(ctx, dmalloc(&ctx->shade, want_px));
     AXR_CUDA(ctx, dmalloc(&ctx->clip_px, want_px));
+    AXR_CUDA(ctx, dmalloc(&ctx->rec, (size_t)kRecFloat4 * want_rec));
+    ctx->rec_cap = want_rec;
     ctx->large_cap = want_tris;
     ctx->item_cap = want_items;
     ctx->vcap = want_verts;
@@ -178,7 +184,7 @@ DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffe
     p.u = u;
     p.scratch = DevScratch{ctx->counters, ctx->large, ctx->items, ctx->vscreen, ctx->vattr,
                            ctx->shade, ctx->clip_px, ctx->large_cap, ctx->item_cap, ctx->vcap, ctx->px_cap,
-                           ctx->collect_stats, 0};
+                           ctx->collect_stats, 0, nullptr, ctx->rec};
     p.small_max_pixels = ctx->small_max_pixels;
     return p;
 }
@@ -689,7 +695,9 @@ axr_status axr_stats_read(axr_context* ctx, axr_draw_stats* out) {
     out->fragments = c.stat_fragments;
     out->large = c.stat_large;
     out->tiles = c.stat_tiles;
-    AXR_CUDA(ctx, cudaMemset(&ctx->counters->stat_triangles, 0, 4 * sizeof(unsigned long long)));
+    out->tested = c.stat_tested;
+    out->shaded = c.stat_shaded;
+    AXR_CUDA(ctx, cudaMemset(&ctx->counters->stat_triangles, 0, 6 * sizeof(unsigned long long)));
     return AXR_OK;
 }
 

@@ -99,7 +99,8 @@ struct axr_context {
     float4* vattr = nullptr;
     uint2* shade = nullptr;
     uint2* clip_px = nullptr;
-    uint32_t large_cap = 0, item_cap = 0, vcap = 0, px_cap = 0;
+    float4* rec = nullptr;  // shading records (kRecFloat4 per face in draw order)
+    uint32_t large_cap = 0, item_cap = 0, vcap = 0, px_cap = 0, rec_cap = 0;
     int collect_stats = 0;
     int small_max_pixels = 64;
     // batched form: per density class, the largest pixel box rasterised per thread

@@ -225,7 +225,10 @@ __device__ uint32_t tile_scan(const DrawParams& p, const UnitInfo& ui, const Til
     }
     if (dirty && lane == 0) {
         t.tile_flag[c.tile] = 0u;
-        if (stats) atomicAdd(&counters->stat_tiles, 1ull);
+        if (stats) {
+            atomicAdd(&counters->stat_tiles, 1ull);
+            atomicAdd(&counters->stat_shaded, (unsigned long long)(nwin + nclip));
+        }
     }
     return nwin | (nclip << 16);
 }
@@ -253,12 +256,9 @@ __device__ __forceinline__ void shade_winner(const DrawParams& p, const UnitInfo
     const int gx = c.tx * kTile + (int)(pix & 15u), gy = c.ty * kTile + (int)(pix >> 4);
     const size_t idx = (size_t)gy * (size_t)t.width + (size_t)gx;
     const float old = c.clear_d ? ui.clear_depth : t.depth[idx];
-    Screen s;
-    VSOut vo[3];
-    const uint32_t material = winner_inputs<S, true>(p, tag, s, vo);
     uint32_t bgra = 0u;
     float z = 0.0f;
-    const bool ok = shade_pixel<S>(p, gx, gy, material, s, vo, old, bgra, z);
+    const bool ok = shade_unclipped<S, true>(p, tag, gx, gy, old, bgra, z);
     tile_put(t, ui, c, stage, pix, idx, ok, bgra, z);
 }
 
@@ -328,7 +328,7 @@ __device__ __forceinline__ void vertex_unit(const DrawParams& p, const UnitInfo&
 // kCoherent: the vertex cache was written earlier in the same launch
 template <bool kCoherent>
 __device__ __forceinline__ void face_unit(const DrawParams& p, const UnitInfo& ui, DevCounters* c, bool stats) {
-    GeomStats st = {0, 0, 0};
+    GeomStats st = {0, 0, 0, 0};
     uint32_t single_tile = kNoTile;
     const uint32_t o = ui.local * kFaceUnit + threadIdx.x;
     if (o < p.mesh.num_drawn) geometry_one<kCoherent>(p, o, st, single_tile);
@@ -343,7 +343,7 @@ __device__ __forceinline__ void large_items(const BatchParams& bp, bool stats) {
     const uint32_t n_items = min(ld_acquire(&c->item_count), bp.item_cap);
     const uint32_t n_tris = min(ld_acquire(&c->large_count), bp.large_cap);
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    uint32_t frags = 0;
+    uint32_t frags = 0, tested = 0;
     for (uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += warps) {
         const LargeItem item = bp.items[it];
         if (item.tri >= n_tris) continue;  // reserved slot of a triangle rasterised elsewhere
@@ -351,11 +351,13 @@ __device__ __forceinline__ void large_items(const BatchParams& bp, bool stats) {
         Edges e;
         uint32_t tag;
         load_large(&bp.large[item.tri], e, tag);
-        large_tile(t, e, tag, item.tile, frags);
+        large_tile(t, e, tag, item.tile, frags, tested);
     }
     if (stats) {
         const uint32_t f = __reduce_add_sync(0xFFFFFFFFu, frags);
+        const uint32_t te = __reduce_add_sync(0xFFFFFFFFu, tested);
         if (lane == 0 && f) atomicAdd(&c->stat_fragments, (unsigned long long)f);
+        if (lane == 0 && te) atomicAdd(&c->stat_tested, (unsigned long long)te);
     }
 }
 
@@ -479,16 +481,19 @@ __global__ void __launch_bounds__(kBatchBlock) batch_large_kernel(const __grid_c
     large_items(bp, bp.collect_stats != 0);
 }
 
-// Tile pass of the phased form: one CTA per 8 tiles (one per warp). Each warp scans its
-// tile, then all 256 threads shade the CTA's winners together (balanced across the eight
-// tiles), then each warp finishes its tile.
+// Tile pass of the phased form: one CTA per tile unit of tiles_per_warp rounds of 8 tiles
+// (one per warp). Per round each warp scans its tile, then all 256 threads shade the
+// round's winners together (balanced across the eight tiles), then each warp finishes its
+// tile; a warp's two staging buffers alternate after each committed TMA store, so a tile's
+// store overlaps the next round. Tiles without keys and with both planes to clear are
+// cleared directly.
 template <int S>
 __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ __align__(16) DrawParams s_p;
     __shared__ UnitInfo s_u;
-    __shared__ __align__(128) uint32_t s_stage[kBatchWarps][512];
+    __shared__ __align__(128) uint32_t s_stage[kBatchWarps][2][512];
     __shared__ uint8_t s_list[kBatchWarps][256];
-    __shared__ uint32_t s_n[kBatchWarps];
+    __shared__ uint32_t s_n[kBatchWarps], s_buf[kBatchWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stats = bp.collect_stats != 0;
     stage_unit(bp, bp.vert_units + bp.face_units + blockIdx.x, &s_p, &s_u);
@@ -496,37 +501,54 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
     const DrawParams& p = s_p;
     const UnitInfo& ui = s_u;
     const uint32_t ntiles = (uint32_t)p.target.tiles_x * (uint32_t)p.target.tiles_y;
-    const uint32_t tile = ui.local * kUnitWarps + (uint32_t)warp;
+    const uint32_t rounds = bp.tiles_per_warp;
+    const uint32_t first = ui.local * kUnitWarps * rounds;  // round j, warp w: first + 8 j + w
     const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
     const bool full = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth);
-    const TileCtx c = tile_ctx(p.target, ui, tile);
-    bool active = false;  // this warp's tile goes through the staged pass
-    uint32_t n = 0;
-    if (tile < ntiles) {
-        const bool dirty = __shfl_sync(0xFFFFFFFFu, lane == 0 ? ld_volatile(&p.target.tile_flag[tile]) : 0u, 0) != 0u;
-        if (!dirty && full) {
-            clear_tile(p.target, tile, ui.clear_bgra, ui.clear_depth);
-        } else if (dirty || clears) {
-            active = true;
-            n = tile_scan(p, ui, c, dirty, s_stage[warp], s_list[warp], bp.counters, stats);
+    // this warp's flags, one round per lane
+    const uint32_t my = first + (uint32_t)lane * kUnitWarps + (uint32_t)warp;
+    const unsigned dirty_mask = __ballot_sync(
+        0xFFFFFFFFu, (uint32_t)lane < rounds && my < ntiles && ld_volatile(&p.target.tile_flag[my]) != 0u);
+    uint32_t sbuf = 0;  // the buffer this warp stages into; never the newest committed store's
+    for (uint32_t j = 0; j < rounds; ++j) {
+        const uint32_t tile = first + j * kUnitWarps + (uint32_t)warp;
+        uint32_t* stage = s_stage[warp][sbuf];
+        const TileCtx c = tile_ctx(p.target, ui, tile);
+        bool active = false;
+        uint32_t n = 0;
+        if (tile < ntiles) {
+            const bool dirty = (dirty_mask >> j) & 1u;
+            if (!dirty && full) {
+                clear_tile(p.target, tile, ui.clear_bgra, ui.clear_depth);
+            } else if (dirty || clears) {
+                active = true;
+                if (lane == 0) tma_wait_read_1();  // an older store from this buffer has read it
+                __syncwarp();
+                n = tile_scan(p, ui, c, dirty, stage, s_list[warp], bp.counters, stats);
+            }
         }
-    }
-    if (lane == 0) s_n[warp] = n & 0xFFFFu;
-    __syncthreads();
-    uint32_t pre[kBatchWarps + 1];
-    pre[0] = 0;
+        if (lane == 0) {
+            s_n[warp] = n & 0xFFFFu;
+            s_buf[warp] = sbuf;
+        }
+        __syncthreads();
+        uint32_t pre[kBatchWarps + 1];
+        pre[0] = 0;
 #pragma unroll
-    for (int w = 0; w < kBatchWarps; ++w) pre[w + 1] = pre[w] + s_n[w];
-    for (uint32_t q = threadIdx.x; q < pre[kBatchWarps]; q += kBatchBlock) {
-        int w = 0;
+        for (int w = 0; w < kBatchWarps; ++w) pre[w + 1] = pre[w] + s_n[w];
+        for (uint32_t q = threadIdx.x; q < pre[kBatchWarps]; q += kBatchBlock) {
+            int w = 0;
 #pragma unroll
-        for (int k = 1; k < kBatchWarps; ++k) w += q >= pre[k] ? 1 : 0;
-        const TileCtx cw = tile_ctx(p.target, ui, ui.local * kUnitWarps + (uint32_t)w);
-        shade_winner<S>(p, ui, cw, s_stage[w], s_list[w][q - pre[w]]);
+            for (int k = 1; k < kBatchWarps; ++k) w += q >= pre[k] ? 1 : 0;
+            const TileCtx cw = tile_ctx(p.target, ui, first + j * kUnitWarps + (uint32_t)w);
+            shade_winner<S>(p, ui, cw, s_stage[w][s_buf[w]], s_list[w][q - pre[w]]);
+        }
+        __syncthreads();
+        if (active && tile_finish<S>(p, ui, &bp.draws[ui.draw], c, stage, s_list[warp], n >> 16)) sbuf ^= 1u;
+        __syncthreads();  // s_list, s_n and s_buf are rewritten by the next round
     }
-    __syncthreads();
-    if (active) tile_finish<S>(p, ui, &bp.draws[ui.draw], c, s_stage[warp], s_list[warp], n >> 16);
-    if (lane == 0) tma_wait_all();
+    // the staging buffers must have been read before the CTA exits
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 template <int S>

@@ -120,7 +120,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         pixels += (uint64_t)d.framebuffer->width * d.framebuffer->height;
         tiles += (uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y;
         const size_t V = d.mesh->num_vertices;
-        cache_bytes += align256(16 * V) + align256(16 * V * (size_t)vattr_float4s(d.shader.kind));
+        cache_bytes += align256(16 * V) + align256(16 * V * (size_t)vattr_float4s(d.shader.kind)) +
+                       align256(16 * (size_t)kRecFloat4 * d.mesh->num_drawn);
     }
     // shared large-triangle lists: a triangle that finds them full is rasterised by its own
     // thread instead, so the sizes trade memory for speed only
@@ -186,8 +187,10 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             cache += align256(16 * (size_t)m->num_vertices);
             float4* vattr = reinterpret_cast<float4*>(cache);
             cache += align256(16 * (size_t)m->num_vertices * (size_t)vattr_float4s(d.shader.kind));
+            float4* rec = reinterpret_cast<float4*>(cache);
+            cache += align256(16 * (size_t)kRecFloat4 * m->num_drawn);
             p.scratch = DevScratch{ctx->counters, d_large, d_items, vscreen, vattr, nullptr, nullptr,
-                                   large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw};
+                                   large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw, rec};
             p.small_max_pixels = ctx->tune_small[density_class(d)];
             p.draw = (uint32_t)k;
             bd.flags = (d.clear_flags & AXR_DRAW_CLEAR_COLOR ? kBatchClearColor : 0u) |

@@ -8,6 +8,7 @@
 //   UnitRef[units]        per work unit (vertex units, then face units, then tile units):
 //                         the draw it belongs to and its index inside the draw
 //   vertex caches         per draw: vscreen[V] float4 + vattr[n*V] float4 (n = VAttr<S>::n)
+//                         + shading records (kRecFloat4 float4 per face in draw order)
 //   LargeTri[large_cap], large_draw[large_cap], LargeItem[item_cap]: shared by all draws
 // Work units: 256 vertices (vertex phase), 256 faces in draw order (geometry phase),
 // 8 x tiles_per_warp tiles of 16x16 (key-scan + shade phase); the large-triangle phase
@@ -83,6 +84,6 @@ struct BatchParams {
 constexpr int kFormPersistent = 0;
 constexpr int kFormPhased = 1;
 constexpr uint32_t kPersistentTilesPerWarp = 8;
-constexpr uint32_t kPhasedTilesPerWarp = 1;
+constexpr uint32_t kPhasedTilesPerWarp = 4;
 
 }  // namespace axr

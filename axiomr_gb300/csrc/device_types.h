@@ -112,6 +112,8 @@ struct DevCounters {
     unsigned long long stat_fragments;   // covered (triangle, pixel) pairs
     unsigned long long stat_large;       // triangles sent to the tile rasteriser
     unsigned long long stat_tiles;       // dirty tiles resolved
+    unsigned long long stat_tested;      // (triangle, pixel) coverage tests evaluated
+    unsigned long long stat_shaded;      // winning fragments shaded
 };
 
 constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
@@ -140,9 +142,16 @@ struct DevScratch {
     int32_t collect_stats;
     int32_t pad_;
     uint32_t* large_draw;     // batched draws: draw index of each LargeTri slot (NULL per draw)
+    float4* rec;              // shading records, kRecFloat4 float4 per draw-order position
 };
 
-struct DrawParams {
+// Shading record of an unclipped triangle that can win a pixel, written by the geometry
+// step at its draw-order position and read by the shading step in place of re-deriving the
+// setup from the face: edge terms, 1/area, vertex depths, x_lo (the row-start rule of
+// eval_pixel), material and the three vertex indices (for the cached vertex outputs).
+constexpr int kRecFloat4 = 5;
+
+struct alignas(16) DrawParams {
     DevMesh mesh;
     DevTarget target;
     DevUniforms u;

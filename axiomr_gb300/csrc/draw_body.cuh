@@ -13,6 +13,13 @@ namespace {
 
 constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
+// Tag bit of an unclipped triangle that left a shading record (clipped triangles use bits
+// 0-3 for 8 + their clip index; an unclipped one has them free). Both shading paths give
+// the same bits; the record saves re-deriving the setup, which pays off when the
+// triangle's box holds at least kRecMinPixels pixels.
+constexpr uint32_t kRecTag = 1u;
+constexpr int kRecMinPixels = 16;
+
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
 
 // A tile that holds at least one depth key is flagged for the key scan (a plain store:
@@ -32,7 +39,7 @@ __device__ __forceinline__ bool write_key(const DevTarget& t, int px, int py, fl
 }
 
 struct GeomStats {
-    uint32_t tris, frags, large;
+    uint32_t tris, frags, large, tested;
 };
 
 // Rasterise a small triangle's pixel box in this thread; returns whether any key was
@@ -56,6 +63,7 @@ __device__ bool raster_box(const DevTarget& t, const Edges& e, uint32_t tag, Geo
                 r0[k] = fadd(fadd(as[k], fmul(e.b[k], fpy)), e.c[k]);
                 r8[k] = fadd(r0[k], fmul(e.a[k], 8.0f));
             }
+            st.tested += (uint32_t)(ex - sx);
             for (int px = sx; px < ex; ++px) {
                 const int i = px - sx;
                 const float lane = (float)(i & 7);
@@ -111,19 +119,48 @@ __device__ __forceinline__ void load_large(const LargeTri* src, Edges& e, uint32
     e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
 }
 
+__device__ __forceinline__ void store_record(const DrawParams& p, uint32_t ordinal, const Edges& e, uint32_t material,
+                                             const uint3& f) {
+    float4* r = p.scratch.rec + (size_t)kRecFloat4 * ordinal;
+    r[0] = make_float4(e.a[0], e.b[0], e.c[0], e.a[1]);
+    r[1] = make_float4(e.b[1], e.c[1], e.a[2], e.b[2]);
+    r[2] = make_float4(e.c[2], e.inv_area, e.z[0], e.z[1]);
+    r[3] = make_float4(e.z[2], __int_as_float(e.x_lo), __uint_as_float(material), __uint_as_float(f.x));
+    r[4] = make_float4(__uint_as_float(f.y), __uint_as_float(f.z), 0.0f, 0.0f);
+}
+
+// kCoherent: the record was written earlier in the same launch (plain loads).
+template <bool kCoherent>
+__device__ __forceinline__ uint32_t load_record(const DrawParams& p, uint32_t ordinal, Edges& e, uint3& f) {
+    const float4* r = p.scratch.rec + (size_t)kRecFloat4 * ordinal;
+    const float4 r0 = ld_cached<kCoherent>(r), r1 = ld_cached<kCoherent>(r + 1), r2 = ld_cached<kCoherent>(r + 2);
+    const float4 r3 = ld_cached<kCoherent>(r + 3), r4 = ld_cached<kCoherent>(r + 4);
+    e.a[0] = r0.x; e.b[0] = r0.y; e.c[0] = r0.z; e.a[1] = r0.w;
+    e.b[1] = r1.x; e.c[1] = r1.y; e.a[2] = r1.z; e.b[2] = r1.w;
+    e.c[2] = r2.x; e.inv_area = r2.y; e.z[0] = r2.z; e.z[1] = r2.w;
+    e.z[2] = r3.x;
+    e.x_lo = __float_as_int(r3.y);
+    f = make_uint3(__float_as_uint(r3.w), __float_as_uint(r4.x), __float_as_uint(r4.y));
+    return __float_as_uint(r3.z);
+}
+
 // One triangle that survived clipping: cull, set up, then rasterise it here or queue its
 // tiles. *single_tile receives the one tile a small triangle wrote to (the caller marks
 // it after deduplicating across the warp); boxes spanning several tiles are marked here.
+// An unclipped triangle that can win a pixel leaves its shading record (face f, material).
 __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag, GeomStats& st,
-                              uint32_t* single_tile) {
+                              uint32_t* single_tile, const uint3& f, uint32_t material) {
     if (is_backface(s)) return;
     ++st.tris;
     Edges e;
     if (!edge_setup(s, p.target.width, p.target.height, e)) return;
     const int npx = (e.x_hi - e.x_lo) * (e.y_hi - e.y_lo);
+    const bool record = (tag & 8u) == 0u && npx >= kRecMinPixels;
+    if (record) tag |= kRecTag;
     DevCounters* c = p.scratch.counters;
     if (npx <= p.small_max_pixels) {
         if (raster_box(p.target, e, tag, st)) {
+            if (record) store_record(p, tag >> 4, e, material, f);
             uint32_t ntx;
             if (tiles_of(e, ntx) == 1u && *single_tile == kNoTile)
                 *single_tile = tile_of(p.target, e.x_lo, e.y_lo);
@@ -137,6 +174,7 @@ __device__ void emit_triangle(const DrawParams& p, const Screen& s, uint32_t tag
     const uint32_t slot = atomicAdd(&c->large_count, 1u);
     const uint32_t base = atomicAdd(&c->item_count, nt);
     const uint32_t icap = p.scratch.item_cap;
+    if (record) store_record(p, tag >> 4, e, material, f);
     if (slot < p.scratch.large_cap && base + nt <= icap && base + nt > base) {
         store_large(&p.scratch.large[slot], e, tag);
         if (p.scratch.large_draw) p.scratch.large_draw[slot] = p.draw;
@@ -188,7 +226,7 @@ __device__ __forceinline__ void geometry_one(const DrawParams& p, uint32_t o, Ge
         s.x[1] = g1.x; s.y[1] = g1.y; s.z[1] = g1.z;
         s.x[2] = g2.x; s.y[2] = g2.y; s.z[2] = g2.z;
         screen_bbox(s);
-        emit_triangle(p, s, o << 4, st, &single_tile);
+        emit_triangle(p, s, o << 4, st, &single_tile, f, fr.material);
     } else if (cls < 0) {
         CVClip a[kMaxClipVerts], b[kMaxClipVerts];
         a[0].clip = load_clip(p.mesh, p.u.mvp, f.x);
@@ -201,7 +239,7 @@ __device__ __forceinline__ void geometry_one(const DrawParams& p, uint32_t o, Ge
             screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width,
                          p.target.height, s);
             uint32_t tile = kNoTile;
-            emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile);
+            emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile, f, fr.material);
             if (tile != kNoTile) mark_tile(p.target, tile);
         }
     }
@@ -216,11 +254,12 @@ __device__ __forceinline__ void geometry_warp_tail(const DevTarget& t, DevCounte
     if (stats) {
         const unsigned full = 0xFFFFFFFFu;
         uint32_t tr = __reduce_add_sync(full, st.tris), fr = __reduce_add_sync(full, st.frags);
-        uint32_t l = __reduce_add_sync(full, st.large);
+        uint32_t l = __reduce_add_sync(full, st.large), te = __reduce_add_sync(full, st.tested);
         if ((threadIdx.x & 31) == 0) {
             if (tr) atomicAdd(&c->stat_triangles, (unsigned long long)tr);
             if (fr) atomicAdd(&c->stat_fragments, (unsigned long long)fr);
             if (l) atomicAdd(&c->stat_large, (unsigned long long)l);
+            if (te) atomicAdd(&c->stat_tested, (unsigned long long)te);
         }
     }
 }
@@ -228,7 +267,7 @@ __device__ __forceinline__ void geometry_warp_tail(const DevTarget& t, DevCounte
 // One large-triangle work item: the warp evaluates the 256 pixels of tile `item_tile` of
 // the triangle's tile box, 8 per lane, and flags the tile if a key was written.
 __device__ __forceinline__ void large_tile(const DevTarget& t, const Edges& e, uint32_t tag, uint32_t item_tile,
-                                           uint32_t& frags) {
+                                           uint32_t& frags, uint32_t& tested) {
     const int lane = threadIdx.x & 31;
     uint32_t ntx;
     tiles_of(e, ntx);
@@ -240,6 +279,7 @@ __device__ __forceinline__ void large_tile(const DevTarget& t, const Edges& e, u
     for (int r = 0; r < 8; ++r) {
         const int py = ty * kTile + (lane >> 4) + 2 * r;
         if (px >= e.x_lo && px < e.x_hi && py >= e.y_lo && py < e.y_hi) {
+            ++tested;
             PixelEval pe = eval_pixel(e, px, py);
             if (pe.covered) {
                 ++frags;
@@ -250,8 +290,8 @@ __device__ __forceinline__ void large_tile(const DevTarget& t, const Edges& e, u
     if (__any_sync(0xFFFFFFFFu, wrote) && lane == 0) mark_tile(t, (uint32_t)ty * (uint32_t)t.tiles_x + (uint32_t)tx);
 }
 
-// Winner inputs of an unclipped tag: screen positions from the vertex cache and the
-// cached vertex-shader outputs.
+// Winner inputs of an unclipped tag without a record: screen positions from the vertex
+// cache and the cached vertex-shader outputs.
 template <int S, bool kCoherent = false>
 __device__ __forceinline__ uint32_t winner_inputs(const DrawParams& p, uint32_t tag, Screen& s, VSOut* vo) {
     const FaceRef fr = face_of(p.mesh, tag >> 4);
@@ -267,6 +307,18 @@ __device__ __forceinline__ uint32_t winner_inputs(const DrawParams& p, uint32_t 
     }
     screen_bbox(s);
     return fr.material;
+}
+
+// Winner inputs of an unclipped tag: its shading record and the cached vertex-shader
+// outputs of its three vertices. Returns the material.
+template <int S, bool kCoherent = false>
+__device__ __forceinline__ uint32_t record_inputs(const DrawParams& p, uint32_t tag, Edges& e, VSOut* vo) {
+    uint3 f;
+    const uint32_t material = load_record<kCoherent>(p, tag >> 4, e, f);
+    const uint32_t vi[3] = {f.x, f.y, f.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) vo[k] = unpack_vsout<S, kCoherent>(&p.scratch.vattr[(size_t)VAttr<S>::n * vi[k]]);
+    return material;
 }
 
 // Winner inputs of a clipped tag: the clipper re-run on the face's raw vertex attributes
@@ -301,6 +353,36 @@ __device__ __forceinline__ bool shade_pixel(const DrawParams& p, int px, int py,
                                             const VSOut* vo, float old_depth, uint32_t& bgra, float& z) {
     Edges e;
     if (!edge_setup(s, p.target.width, p.target.height, e)) return false;
+    const PixelEval r = eval_pixel(e, px, py);
+    if (!(r.z < old_depth)) return false;
+    const f4 col = fragment_shader<S>(p.u, p.mesh.materials[material], mk3(r.alpha, r.beta, r.gamma), vo);
+    bgra = pack_bgra(col);
+    z = r.z;
+    return true;
+}
+
+}  // namespace
+}  // namespace axr
+
+namespace axr {
+namespace {
+
+// Fragment of the unclipped winner `tag` at (px, py): the setup from its shading record
+// when it has one, else re-derived from the face; then exact barycentrics and depth, the
+// strict merge test against `old_depth` and the shader. Returns whether it is written.
+template <int S, bool kCoherent = false>
+__device__ __forceinline__ bool shade_unclipped(const DrawParams& p, uint32_t tag, int px, int py, float old_depth,
+                                                uint32_t& bgra, float& z) {
+    VSOut vo[3];
+    Edges e;
+    uint32_t material;
+    if (tag & kRecTag) {
+        material = record_inputs<S, kCoherent>(p, tag, e, vo);
+    } else {
+        Screen s;
+        material = winner_inputs<S, kCoherent>(p, tag, s, vo);
+        if (!edge_setup(s, p.target.width, p.target.height, e)) return false;
+    }
     const PixelEval r = eval_pixel(e, px, py);
     if (!(r.z < old_depth)) return false;
     const f4 col = fragment_shader<S>(p.u, p.mesh.materials[material], mk3(r.alpha, r.beta, r.gamma), vo);

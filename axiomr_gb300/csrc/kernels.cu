@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kBlock) vertex_kernel(const __grid_constant__ 
 }
 
 __global__ void __launch_bounds__(kBlock, AXR_GEOMETRY_MIN_BLOCKS) geometry_kernel(const __grid_constant__ DrawParams p) {
-    GeomStats st = {0, 0, 0};
+    GeomStats st = {0, 0, 0, 0};
     uint32_t single_tile = kNoTile;
     const uint32_t o = blockIdx.x * kBlock + threadIdx.x;
     if (o < p.mesh.num_drawn) geometry_one(p, o, st, single_tile);
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
     if (n_items == 0) return;
     const uint32_t n_tris = min(ld_volatile(&c->large_count), p.scratch.large_cap);
     const int lane = threadIdx.x & 31;
-    uint32_t frags = 0;
+    uint32_t frags = 0, tested = 0;
     for (;;) {
         uint32_t first = 0;
         if (lane == 0) first = atomicAdd(&c->item_head, kItemsPerGrab);
@@ -78,12 +78,14 @@ __global__ void __launch_bounds__(kBlock) large_kernel(const __grid_constant__ D
             Edges e;
             uint32_t tag;
             load_large(&p.scratch.large[item.tri], e, tag);
-            large_tile(p.target, e, tag, item.tile, frags);
+            large_tile(p.target, e, tag, item.tile, frags, tested);
         }
     }
     if (p.scratch.collect_stats) {
         uint32_t f = __reduce_add_sync(0xFFFFFFFFu, frags);
+        const uint32_t te = __reduce_add_sync(0xFFFFFFFFu, tested);
         if (lane == 0 && f) atomicAdd(&c->stat_fragments, (unsigned long long)f);
+        if (lane == 0 && te) atomicAdd(&c->stat_tested, (unsigned long long)te);
     }
 }
 
@@ -159,16 +161,19 @@ __global__ void __launch_bounds__(kBlock) scan_kernel(const __grid_constant__ Dr
             }
             if (lane == 0) {
                 t.tile_flag[tile] = 0u;
-                if (p.scratch.collect_stats) atomicAdd(&c->stat_tiles, 1ull);
+                if (p.scratch.collect_stats) {
+                    atomicAdd(&c->stat_tiles, 1ull);
+                    atomicAdd(&c->stat_shaded, (unsigned long long)(ns + nc));
+                }
             }
         }
         __syncthreads();
     }
 }
 
-// Dense shading of the covered pixels whose winner is unclipped: the winner is re-derived
-// from its tag (face -> cached vertex screen positions and shader outputs), its
-// barycentrics recomputed exactly and the fragment shaded once.
+// Dense shading of the covered pixels whose winner is unclipped: the winner's setup (from
+// its shading record, or re-derived from the face and the vertex cache) gives its exact
+// barycentrics and depth, and the fragment is shaded once.
 template <int S>
 __global__ void __launch_bounds__(kBlock) shade_kernel(const __grid_constant__ DrawParams p) {
     DevCounters* c = p.scratch.counters;
@@ -178,12 +183,9 @@ __global__ void __launch_bounds__(kBlock) shade_kernel(const __grid_constant__ D
         const uint2 w = p.scratch.shade[q];
         const size_t idx = w.x;
         const int px = (int)(idx % (size_t)t.width), py = (int)(idx / (size_t)t.width);
-        Screen s;
-        VSOut vo[3];
-        const uint32_t material = winner_inputs<S>(p, w.y, s, vo);
         uint32_t bgra;
         float z;
-        if (shade_pixel<S>(p, px, py, material, s, vo, t.depth[idx], bgra, z)) {
+        if (shade_unclipped<S>(p, w.y, px, py, t.depth[idx], bgra, z)) {
             t.color[idx] = bgra;
             t.depth[idx] = z;
         }

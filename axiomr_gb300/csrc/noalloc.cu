@@ -13,7 +13,7 @@
 //
 // Limits: at most kNoAllocMaxVertices vertices, kNoAllocMaxFaces drawn faces and
 // kNoAllocMaxPixels framebuffer pixels per call; larger draws are rejected with
-// AXR_E_CAPACITY. The array (about 27 MiB) is reserved on every GPU that loads the library
+// AXR_E_CAPACITY. The array (about 32 MiB) is reserved on every GPU that loads the library
 // and stays reserved until the process exits.
 //
 // Set-up: the first call on each device looks up the array's device address with
@@ -42,7 +42,8 @@ constexpr size_t kOffVscreen = align256(kOffItems + sizeof(axr::LargeItem) * kNo
 constexpr size_t kOffVattr = align256(kOffVscreen + sizeof(float4) * kNoAllocMaxVertices);
 constexpr size_t kOffShade = align256(kOffVattr + 4 * sizeof(float4) * kNoAllocMaxVertices);
 constexpr size_t kOffClip = align256(kOffShade + sizeof(uint2) * kNoAllocMaxPixels);
-constexpr size_t kNoAllocBytes = align256(kOffClip + sizeof(uint2) * kNoAllocMaxPixels);
+constexpr size_t kOffRec = align256(kOffClip + sizeof(uint2) * kNoAllocMaxPixels);
+constexpr size_t kNoAllocBytes = align256(kOffRec + sizeof(float4) * axr::kRecFloat4 * kNoAllocMaxFaces);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -108,7 +109,7 @@ extern "C" axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* me
                                reinterpret_cast<uint2*>(base + kOffShade),
                                reinterpret_cast<uint2*>(base + kOffClip),
                                kNoAllocMaxFaces, kNoAllocMaxItems, kNoAllocMaxVertices, kNoAllocMaxPixels,
-                               0, 0};
+                               0, 0, nullptr, reinterpret_cast<float4*>(base + kOffRec)};
         p.small_max_pixels = ctx->small_max_pixels;
         // the array keeps the previous call's contents: start from zeroed counters
         e = cudaMemsetAsync(counters, 0, sizeof(DevCounters), ctx->stream);

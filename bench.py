@@ -57,6 +57,11 @@ WORKLOADS["serve"] = (None, "open-loop Poisson arrivals; 90% requests of the sma
                             "triangles, 3840x2160, Gouraud; one of 64 seeded soups), 10% heightfields (2,093,058 "
                             "triangles, 1920x1080, Blinn-Phong, random camera azimuth); 40 GB residency budget")
 BATCH_REF_SAMPLE = 16  # draws of the mixed batch the CPU arms render per step (every 32nd)
+# FP32 operations of fragment_shader<kBlinnPhong> (axiomr_gb300/csrc/shade.cuh), counted from
+# the source: uv barycentric 10, texel scale 6, normal barycentric + normalize 25, world
+# position 15, view direction 13, half vector 13, ambient 3, diffuse 9, specular 14,
+# combine 9, quantisation 12.
+K_BLINN_PHONG = 129
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -614,10 +619,16 @@ def run_batch(args, dist: Dist):
     nl = max(1, pr["batch_launches"])
     phase_ms = {k: pr[f"batch_{k}_ms"] / nl for k in ("vertex", "face", "large", "tile")}
 
+    fp32_tflops = ctx.fp32_peak_tflops()
     hbm_peak, peak_kind = measured_peaks()
     ms = total_ms / len(step_ms)
     frags = float(st["fragments"])
     algo = batch_algo_bytes(scenes, frags)
+    # fragment ALU work (SURVEY's frame roofline): FP32 operations of the Blinn-Phong
+    # fragment functor counted from its source (K_BLINN_PHONG) per shaded fragment, plus
+    # three edge evaluations and three compares (9) per tested pixel
+    alu_flop = K_BLINN_PHONG * float(st["shaded"]) + 9.0 * float(st["tested"])
+    alu_tflops = alu_flop / (ms * 1e-3) / 1e12
     achieved = algo / (ms * 1e-3) / 1e9
     faces = info["faces"]
     pb = batch_phase_bytes(scenes, frags, int(info["tiles"]))
@@ -630,14 +641,17 @@ def run_batch(args, dist: Dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
-        "config": {"workload": f"batch: {desc}", "form": "batched: one persistent cooperative launch per step "
-                   "(clears fused), replayed from a CUDA graph",
+        "config": {"workload": f"batch: {desc}",
+                   "form": ("batched, phased: four launches per step over the work units of all draws"
+                            if info["form"] == 1 else "batched, persistent: one cooperative launch per step")
+                   + " (clears fused into the tile pass), replayed from a CUDA graph",
                    "frames_per_step": n, "l2": "flushed before every timed step (256 MiB write, outside the events)",
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
                    "tuning_small_max_pixels": tuning},
         "gfrag_per_s": round(frags * value / n / 1e9, 3),
         "mtri_per_s": round(faces * value / n / 1e6, 2),
-        "fragments_per_step": int(frags), "triangles_per_step": int(st["triangles"]), "faces_per_step": int(faces),
+        "fragments_per_step": int(frags), "shaded_per_step": int(st["shaded"]), "tested_per_step": int(st["tested"]),
+        "triangles_per_step": int(st["triangles"]), "faces_per_step": int(faces),
         "pixels_per_step": int(info["pixels"]),
         "plain": {"value": round(plain_value, 2), "unit": "frames/s", "ms_per_step": round(sum(plain_ms) / len(plain_ms), 4),
                   "form": "per draw: clearColor, clearDepth, drawMesh (9 launches), replayed from a CUDA graph",
@@ -656,10 +670,16 @@ def run_batch(args, dist: Dist):
                      "frac": round(dom_achieved / hbm_peak, 4), "traffic": profiled_traffic(kernel_of[dom], "batch"),
                      "algorithmic_bytes": pb[dom], "launch_us": round(phase_ms[dom] * 1e3, 2),
                      "phase_us": {k: round(v * 1e3, 2) for k, v in phase_ms.items()}},
-        "frame_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                           "frac": round(achieved / hbm_peak, 4), "algorithmic_bytes": algo,
-                           "definition": "per draw V*32 + F*12 + W*H*8 + min(texture, 4 per covered fragment), "
-                                         "over the whole step"},
+        "frame_roofline": {"bound": "hbm" if achieved / hbm_peak >= alu_tflops / fp32_tflops else "alu",
+                           "hbm": {"achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                                   "frac": round(achieved / hbm_peak, 4), "algorithmic_bytes": algo,
+                                   "definition": "per draw V*32 + F*12 + W*H*8 + min(texture, 4 per covered "
+                                                 "fragment), over the whole step"},
+                           "alu": {"achieved": round(alu_tflops, 3), "peak": round(fp32_tflops, 2), "unit": "TFLOP/s",
+                                   "frac": round(alu_tflops / fp32_tflops, 4), "flop": alu_flop,
+                                   "definition": f"{K_BLINN_PHONG} FP32 ops per shaded fragment (Blinn-Phong "
+                                                 "functor) + 9 per tested pixel; peak measured with FMA chains "
+                                                 "(axr_measure_fp32_peak)"}},
         "form": "phased" if info["form"] == 1 else "persistent",
         "clocks": sampler.summary(),
     }

@@ -190,7 +190,7 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
 /* No counterpart in the reference. The same draw as axr_draw_mesh for callers that cannot
  * allocate device memory: a renderer recording its frame into a CUDA graph, a real-time
  * loop that forbids allocator calls after start-up, or a host that owns the device-memory
- * budget. Its scratch lives in one fixed device array inside the library (about 27 MiB,
+ * budget. Its scratch lives in one fixed device array inside the library (about 32 MiB,
  * reserved on every GPU that loads the library until exit), so the call allocates nothing.
  * Limits: 65536 vertices, 65536 drawn faces, 1024*1024 framebuffer pixels; larger draws
  * return AXR_E_CAPACITY. The first call on a device looks up the array's address, so make
@@ -398,6 +398,8 @@ typedef struct axr_draw_stats {
     uint64_t fragments;  /* covered (triangle, pixel) pairs */
     uint64_t large;      /* triangles rasterised by the tile kernel */
     uint64_t tiles;      /* 16x16 tiles resolved */
+    uint64_t tested;     /* (triangle, pixel) coverage tests evaluated */
+    uint64_t shaded;     /* winning fragments shaded (covered pixels after the depth test) */
 } axr_draw_stats;
 axr_status axr_stats_enable(axr_context* ctx, int32_t enable);
 axr_status axr_stats_read(axr_context* ctx, axr_draw_stats* out); /* synchronises, then resets */
@@ -425,6 +427,11 @@ typedef struct axr_profile {
 } axr_profile;
 axr_status axr_profile_enable(axr_context* ctx, int32_t enable);
 axr_status axr_profile_read(axr_context* ctx, axr_profile* out);
+
+/* FP32 issue peak (TFLOP/s) measured on the context's device with independent FMA
+ * chains over a fully occupied grid: the denominator of the fragment-ALU roofline. No
+ * reference counterpart. */
+axr_status axr_measure_fp32_peak(axr_context* ctx, double* tflops);
 
 /* ------------------------------------------------------------------ stage access (tests)
  * Every triangle of a draw that survives clipping and culling, as 14 words each:
