@@ -145,6 +145,7 @@ SIGNATURES = {
     "axr_framebuffer_read": (S, [P, P, P, P]),
     "axr_framebuffer_read_async": (S, [P, P, P, P]),
     "axr_framebuffer_write": (S, [P, P, P, P]),
+    "axr_framebuffers_read_async": (S, [P, C.c_int32, P, P, P]),
     "axr_framebuffer_size": (S, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "axr_framebuffer_device_pointers": (S, [P, PP, PP]),
     "axr_set_shader": (S, [P, P]),

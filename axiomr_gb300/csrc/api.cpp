@@ -226,6 +226,14 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
         axr_status st = cuda_fail(nullptr, e, "context setup");
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
         if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
+    for (int k = 0; k < axr_context::kCopyStreams; ++k) {
+        if (ctx->copy_stream[k]) {
+            cudaStreamSynchronize(ctx->copy_stream[k]);
+            cudaStreamDestroy(ctx->copy_stream[k]);
+        }
+        if (ctx->copy_join[k]) cudaEventDestroy(ctx->copy_join[k]);
+    }
+    if (ctx->copy_fork) cudaEventDestroy(ctx->copy_fork);
         if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
         if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
         dfree(ctx->counters);
@@ -256,6 +264,14 @@ void axr_context_destroy(axr_context* ctx) {
     free_scratch(ctx);
     if (ctx->aux.stream) cudaStreamSynchronize(ctx->aux.stream);
     if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
+    for (int k = 0; k < axr_context::kCopyStreams; ++k) {
+        if (ctx->copy_stream[k]) {
+            cudaStreamSynchronize(ctx->copy_stream[k]);
+            cudaStreamDestroy(ctx->copy_stream[k]);
+        }
+        if (ctx->copy_join[k]) cudaEventDestroy(ctx->copy_join[k]);
+    }
+    if (ctx->copy_fork) cudaEventDestroy(ctx->copy_fork);
     if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
     if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -521,6 +537,37 @@ static axr_status fb_read(axr_context* ctx, const axr_framebuffer* fb, uint8_t* 
 
 axr_status axr_framebuffer_read(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth) {
     return fb_read(ctx, fb, bgra, depth, true);
+}
+
+axr_status axr_framebuffers_read_async(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
+                                       uint8_t* const* bgra, float* const* depth) {
+    if (!ctx || count < 0 || (count > 0 && !fbs)) return fail(ctx, AXR_E_INVALID, "bad framebuffer list");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    if (!ctx->copy_fork) {
+        AXR_CUDA(ctx, cudaEventCreateWithFlags(&ctx->copy_fork, cudaEventDisableTiming));
+        for (int k = 0; k < axr_context::kCopyStreams; ++k) {
+            AXR_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream[k], cudaStreamNonBlocking));
+            AXR_CUDA(ctx, cudaEventCreateWithFlags(&ctx->copy_join[k], cudaEventDisableTiming));
+        }
+    }
+    // the copies start after the work already enqueued on the context stream, and the
+    // context stream continues after all of them
+    AXR_CUDA(ctx, cudaEventRecord(ctx->copy_fork, ctx->stream));
+    for (int k = 0; k < axr_context::kCopyStreams; ++k) AXR_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream[k], ctx->copy_fork, 0));
+    for (int32_t i = 0; i < count; ++i) {
+        const axr_framebuffer* fb = fbs[i];
+        if (!fb) return fail(ctx, AXR_E_INVALID, "framebuffer %d is NULL", i);
+        const size_t n = (size_t)fb->width * fb->height;
+        cudaStream_t st = ctx->copy_stream[i % axr_context::kCopyStreams];
+        if (bgra && bgra[i]) AXR_CUDA(ctx, cudaMemcpyAsync(bgra[i], fb->color, n * 4, cudaMemcpyDeviceToHost, st));
+        if (depth && depth[i]) AXR_CUDA(ctx, cudaMemcpyAsync(depth[i], fb->depth, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    for (int k = 0; k < axr_context::kCopyStreams; ++k) {
+        AXR_CUDA(ctx, cudaEventRecord(ctx->copy_join[k], ctx->copy_stream[k]));
+        AXR_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_join[k], 0));
+    }
+    return AXR_OK;
 }
 
 axr_status axr_framebuffer_read_async(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth) {

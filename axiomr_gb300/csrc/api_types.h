@@ -82,6 +82,11 @@ struct axr_context {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     axr::AuxStream aux{};  // side stream + fork/join events for the clipped-winner pass
+    // read-back streams of axr_framebuffers_read_async (created on first use): copies of many
+    // framebuffers are spread over them so that several copy engines run at once
+    static constexpr int kCopyStreams = 4;
+    cudaStream_t copy_stream[kCopyStreams] = {};
+    cudaEvent_t copy_fork = nullptr, copy_join[kCopyStreams] = {};
     LaunchConfig cfg{};
     std::mutex mu;
     std::string error;

@@ -481,19 +481,22 @@ __global__ void __launch_bounds__(kBatchBlock) batch_large_kernel(const __grid_c
     large_items(bp, bp.collect_stats != 0);
 }
 
-// Tile pass of the phased form: one CTA per tile unit of tiles_per_warp rounds of 8 tiles
-// (one per warp). Per round each warp scans its tile, then all 256 threads shade the
-// round's winners together (balanced across the eight tiles), then each warp finishes its
-// tile; a warp's two staging buffers alternate after each committed TMA store, so a tile's
-// store overlaps the next round. Tiles without keys and with both planes to clear are
-// cleared directly.
+// Tile pass of the phased form: one CTA per unit of 8 x tiles_per_warp consecutive tiles
+// (at most 32). Warp 0 reads the unit's tile flags with one load per lane. Tiles without
+// keys whose two planes are to be cleared are cleared directly by the warps (no staging,
+// no barrier). The other tiles go through the staged pass in rounds of eight, one per
+// warp: each warp scans its tile, then all 256 threads shade the round's winners together
+// (balanced across the eight tiles), then each warp finishes its tile. A warp's two
+// staging buffers alternate after each committed TMA store, so a tile's store overlaps
+// the next round.
 template <int S>
 __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ __align__(16) DrawParams s_p;
     __shared__ UnitInfo s_u;
     __shared__ __align__(128) uint32_t s_stage[kBatchWarps][2][512];
     __shared__ uint8_t s_list[kBatchWarps][256];
-    __shared__ uint32_t s_n[kBatchWarps], s_buf[kBatchWarps];
+    __shared__ uint32_t s_n[kBatchWarps], s_buf[kBatchWarps], s_tile[kBatchWarps];
+    __shared__ uint32_t s_dirty;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stats = bp.collect_stats != 0;
     stage_unit(bp, bp.vert_units + bp.face_units + blockIdx.x, &s_p, &s_u);
@@ -501,35 +504,54 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
     const DrawParams& p = s_p;
     const UnitInfo& ui = s_u;
     const uint32_t ntiles = (uint32_t)p.target.tiles_x * (uint32_t)p.target.tiles_y;
-    const uint32_t rounds = bp.tiles_per_warp;
-    const uint32_t first = ui.local * kUnitWarps * rounds;  // round j, warp w: first + 8 j + w
+    const uint32_t unit = kUnitWarps * bp.tiles_per_warp;  // <= 32
+    const uint32_t first = ui.local * unit;
+    const uint32_t count = min(unit, ntiles - first);
+    if (warp == 0) {
+        const bool f = (uint32_t)lane < count && ld_volatile(&p.target.tile_flag[first + (uint32_t)lane]) != 0u;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
+        if (lane == 0) s_dirty = m;
+    }
+    __syncthreads();
+    const unsigned all = count >= 32u ? 0xFFFFFFFFu : ((1u << count) - 1u);
+    const unsigned dirty = s_dirty;
     const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
     const bool full = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth);
-    // this warp's flags, one round per lane
-    const uint32_t my = first + (uint32_t)lane * kUnitWarps + (uint32_t)warp;
-    const unsigned dirty_mask = __ballot_sync(
-        0xFFFFFFFFu, (uint32_t)lane < rounds && my < ntiles && ld_volatile(&p.target.tile_flag[my]) != 0u);
+    // key-less tiles with a full clear: direct stores, spread over the warps
+    if (full) {
+        unsigned clean = all & ~dirty;
+        for (int k = 0; clean; ++k) {
+            const int t = __ffs(clean) - 1;
+            clean &= clean - 1u;
+            if ((k & (kBatchWarps - 1)) == warp) clear_tile(p.target, first + (uint32_t)t, ui.clear_bgra, ui.clear_depth);
+        }
+    }
+    // staged tiles: the dirty ones, plus the key-less ones when only one plane is cleared
+    unsigned work = full ? dirty : (clears ? all : dirty);
     uint32_t sbuf = 0;  // the buffer this warp stages into; never the newest committed store's
-    for (uint32_t j = 0; j < rounds; ++j) {
-        const uint32_t tile = first + j * kUnitWarps + (uint32_t)warp;
+    while (work) {
+        // this round: the next eight tiles of `work`, the w-th to warp w
+        int mine = -1;
+#pragma unroll
+        for (int w = 0; w < kBatchWarps; ++w) {
+            if (!work) break;
+            const int t = __ffs(work) - 1;
+            work &= work - 1u;
+            if (w == warp) mine = t;
+        }
+        const uint32_t tile = first + (uint32_t)(mine < 0 ? 0 : mine);
         uint32_t* stage = s_stage[warp][sbuf];
         const TileCtx c = tile_ctx(p.target, ui, tile);
-        bool active = false;
         uint32_t n = 0;
-        if (tile < ntiles) {
-            const bool dirty = (dirty_mask >> j) & 1u;
-            if (!dirty && full) {
-                clear_tile(p.target, tile, ui.clear_bgra, ui.clear_depth);
-            } else if (dirty || clears) {
-                active = true;
-                if (lane == 0) tma_wait_read_1();  // an older store from this buffer has read it
-                __syncwarp();
-                n = tile_scan(p, ui, c, dirty, stage, s_list[warp], bp.counters, stats);
-            }
+        if (mine >= 0) {
+            if (lane == 0) tma_wait_read_1();  // an older store from this buffer has read it
+            __syncwarp();
+            n = tile_scan(p, ui, c, (dirty >> mine) & 1u, stage, s_list[warp], bp.counters, stats);
         }
         if (lane == 0) {
             s_n[warp] = n & 0xFFFFu;
             s_buf[warp] = sbuf;
+            s_tile[warp] = tile;
         }
         __syncthreads();
         uint32_t pre[kBatchWarps + 1];
@@ -540,12 +562,11 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
             int w = 0;
 #pragma unroll
             for (int k = 1; k < kBatchWarps; ++k) w += q >= pre[k] ? 1 : 0;
-            const TileCtx cw = tile_ctx(p.target, ui, first + j * kUnitWarps + (uint32_t)w);
-            shade_winner<S>(p, ui, cw, s_stage[w][s_buf[w]], s_list[w][q - pre[w]]);
+            shade_winner<S>(p, ui, tile_ctx(p.target, ui, s_tile[w]), s_stage[w][s_buf[w]], s_list[w][q - pre[w]]);
         }
         __syncthreads();
-        if (active && tile_finish<S>(p, ui, &bp.draws[ui.draw], c, stage, s_list[warp], n >> 16)) sbuf ^= 1u;
-        __syncthreads();  // s_list, s_n and s_buf are rewritten by the next round
+        if (mine >= 0 && tile_finish<S>(p, ui, &bp.draws[ui.draw], c, stage, s_list[warp], n >> 16)) sbuf ^= 1u;
+        __syncthreads();  // s_list, s_n, s_buf and s_tile are rewritten by the next round
     }
     // the staging buffers must have been read before the CTA exits
     if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");

@@ -264,6 +264,28 @@ __device__ __forceinline__ void geometry_warp_tail(const DevTarget& t, DevCounte
     }
 }
 
+// Whether no pixel of 16x16 tile (tx, ty) inside the triangle's box can test covered.
+// Each edge function is linear, so over the tile's pixel centres it peaks at a corner of
+// their rectangle. eval_pixel's float evaluation of an edge at a centre is within a few
+// units of 2^-24 * M of its exact value, M = |a|(|x|+16) + |b||y| + |c| bounding the
+// magnitudes of its terms, and the corner values here are within 3 such units; if the
+// corner maximum of some edge is below -64 * 2^-24 * M, every evaluated value of that edge
+// in the tile is negative, so the tile holds no covered pixel and is skipped.
+__device__ __forceinline__ bool tile_outside(const Edges& e, int tx, int ty) {
+    const float x0 = (float)max(tx * kTile, e.x_lo) + 0.5f, x1 = (float)min(tx * kTile + kTile, e.x_hi) - 0.5f;
+    const float y0 = (float)max(ty * kTile, e.y_lo) + 0.5f, y1 = (float)min(ty * kTile + kTile, e.y_hi) - 0.5f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = e.a[k], b = e.b[k], c = e.c[k];
+        const float ex = a >= 0.f ? a * x1 : a * x0;  // the larger of a*x0, a*x1
+        const float ey = b >= 0.f ? b * y1 : b * y0;
+        const float emax = (ex + ey) + c;
+        const float m = fabsf(a) * (fabsf(x1) + 16.0f) + fabsf(b) * fabsf(y1) + fabsf(c);
+        if (emax < -64.0f * 5.9604645e-8f * m) return true;
+    }
+    return false;
+}
+
 // One large-triangle work item: the warp evaluates the 256 pixels of tile `item_tile` of
 // the triangle's tile box, 8 per lane, and flags the tile if a key was written.
 __device__ __forceinline__ void large_tile(const DevTarget& t, const Edges& e, uint32_t tag, uint32_t item_tile,
@@ -273,6 +295,7 @@ __device__ __forceinline__ void large_tile(const DevTarget& t, const Edges& e, u
     tiles_of(e, ntx);
     const int tx = (e.x_lo >> 4) + (int)(item_tile % ntx);
     const int ty = (e.y_lo >> 4) + (int)(item_tile / ntx);
+    if (tile_outside(e, tx, ty)) return;
     const int px = tx * kTile + (lane & 15);
     bool wrote = false;
 #pragma unroll

@@ -590,13 +590,15 @@ def run_batch(args, dist: Dist):
                      pinned_like(lib, np.zeros((h, w), np.float32), keep)))
     d2h = sum(a.nbytes + b.nbytes for a, b in outs)
     h2d = n * C.sizeof(api.DrawDesc)
+    fb_arr = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in draws])
+    bgra_arr = (C.c_void_p * n)(*[hb.ctypes.data for hb, _ in outs])
+    depth_arr = (C.c_void_p * n)(*[hd.ctypes.data for _, hd in outs])
 
     def e2e_step():
         api.draw_batch(ctx, draws)
-        for d, (hb, hd) in zip(draws, outs):
-            rc = lib.axr_framebuffer_read_async(ctx.handle, d.framebuffer.handle, hb.ctypes.data, hd.ctypes.data)
-            if rc != 0:
-                raise RuntimeError("axr_framebuffer_read_async failed")
+        rc = lib.axr_framebuffers_read_async(ctx.handle, n, fb_arr, bgra_arr, depth_arr)
+        if rc != 0:
+            raise RuntimeError("axr_framebuffers_read_async failed")
 
     for _ in range(2):
         e2e_step()
@@ -662,7 +664,8 @@ def run_batch(args, dist: Dist):
         "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "path": "axr_draw_batch (draw table from the host) + colour and depth read-back of all 512 "
-                        "framebuffers into pinned memory; meshes and textures resident",
+                        "framebuffers into pinned memory (axr_framebuffers_read_async, 4 copy streams); meshes "
+                        "and textures resident",
                 "gpu_launches_per_step": e2e_launches},
         "gpu_launches": int(info["launches"]) * len(step_ms),
         "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),

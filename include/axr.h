@@ -153,6 +153,13 @@ axr_status axr_framebuffer_clear_depth(axr_context* ctx, axr_framebuffer* fb, fl
 axr_status axr_framebuffer_read(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth);
 /* Enqueue the same copies without waiting (use pinned memory and axr_sync). */
 axr_status axr_framebuffer_read_async(axr_context* ctx, const axr_framebuffer* fb, uint8_t* bgra, float* depth);
+/* The copies of axr_framebuffer_read_async for `count` framebuffers in one call (no
+ * reference counterpart): bgra[i] / depth[i] (either array, or any entry, may be NULL)
+ * receive framebuffer i. The copies run on several internal streams (several copy engines
+ * at once) after the work already enqueued on the context stream; work enqueued later
+ * waits for them. Use pinned memory and axr_sync. */
+axr_status axr_framebuffers_read_async(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
+                                       uint8_t* const* bgra, float* const* depth);
 /* Upload host colour and/or depth into the framebuffer (either may be NULL). */
 axr_status axr_framebuffer_write(axr_context* ctx, axr_framebuffer* fb, const uint8_t* bgra, const float* depth);
 axr_status axr_framebuffer_size(const axr_framebuffer* fb, int32_t* width, int32_t* height);

@@ -200,3 +200,26 @@ def test_batch_argument_errors(ctx):
         api.draw_batch(ctx, [bad])
     api.draw_batch(ctx, [])  # empty batch: nothing to do
     ctx.sync()
+
+
+def test_framebuffers_read_async_matches_single_reads(ctx):
+    import ctypes as C
+
+    scenes = small_batch(count=6, seed=17)
+    draws = api.batch_draws(ctx, scenes)
+    api.draw_batch(ctx, draws)
+    single = [d.framebuffer.read() for d in draws]
+    n = len(draws)
+    outs = [(np.zeros((d.framebuffer.height, d.framebuffer.width, 4), np.uint8),
+             np.zeros((d.framebuffer.height, d.framebuffer.width), np.float32)) for d in draws]
+    fbs = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in draws])
+    bgra = (C.c_void_p * n)(*[o[0].ctypes.data for o in outs])
+    depth = (C.c_void_p * n)(*[o[1].ctypes.data if k % 2 == 0 else None for k, o in enumerate(outs)])
+    assert ctx.lib.axr_framebuffers_read_async(ctx.handle, n, fbs, bgra, depth) == 0
+    ctx.sync()
+    for k in range(n):
+        assert np.array_equal(outs[k][0], single[k][0])
+        if k % 2 == 0:
+            assert np.array_equal(outs[k][1].view(np.uint32), single[k][1].view(np.uint32))
+        else:
+            assert not outs[k][1].any()  # depth not requested
