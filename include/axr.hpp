@@ -12,6 +12,8 @@
 //   setShader / setCamera / setFramebuffer   same
 //   drawMesh(modelMatrix, mesh)              same (model is 16 floats, column-major)
 //   Renderer::drawMesh                       Renderer::drawMesh
+//   (no counterpart)                         Draw / Batch: many draws in one launch set
+//   (no counterpart)                         Server: the continuous-batching request loop
 //
 // Failures throw axr::Error (the reference throws std exceptions too); the C ABI itself
 // never throws. Every object holds the context it was created on.
@@ -253,6 +255,108 @@ public:
 
 private:
     TiledPipeline& pipeline_;
+};
+
+// ---------------------------------------------------------------- batched form
+// One draw of a batch: its own mesh, framebuffer, camera, shader and model matrix; the
+// optional clears run before it (fused into the batch's tile pass).
+struct Draw {
+    const Mesh* mesh = nullptr;
+    Framebuffer* framebuffer = nullptr;
+    const Camera* camera = nullptr;
+    const IShader* shader = nullptr;
+    Mat4 model = identity();
+    bool clear_color = true, clear_depth = true;
+    Color color{0, 0, 0, 255};
+    float depth = std::numeric_limits<float>::infinity();
+
+    axr_draw_desc desc() const {
+        axr_draw_desc d{};
+        d.mesh = mesh->get();
+        d.framebuffer = framebuffer->get();
+        for (int k = 0; k < 16; ++k) d.model[k] = model[(size_t)k];
+        d.camera = camera->desc();
+        d.shader = shader->desc();
+        d.clear_flags = (clear_color ? AXR_DRAW_CLEAR_COLOR : 0u) | (clear_depth ? AXR_DRAW_CLEAR_DEPTH : 0u);
+        d.clear_rgba[0] = color.r;
+        d.clear_rgba[1] = color.g;
+        d.clear_rgba[2] = color.b;
+        d.clear_rgba[3] = color.a;
+        d.clear_depth = depth;
+        return d;
+    }
+};
+
+inline std::vector<axr_draw_desc> descs(const std::vector<Draw>& draws) {
+    std::vector<axr_draw_desc> d;
+    d.reserve(draws.size());
+    for (const Draw& x : draws) d.push_back(x.desc());
+    return d;
+}
+
+// A planned batch: launch() enqueues all its draws (replayable from a CUDA graph).
+class Batch {
+public:
+    Batch(const Context& ctx, const std::vector<Draw>& draws) : ctx_(ctx) {
+        std::vector<axr_draw_desc> d = descs(draws);
+        axr_batch* b = nullptr;
+        check(axr_batch_create(ctx.get(), d.data(), (int32_t)d.size(), &b), ctx.get());
+        batch_.reset(b, [c = ctx_](axr_batch* p) { axr_batch_destroy(c.get(), p); });
+    }
+    void launch() { check(axr_batch_launch(ctx_.get(), batch_.get()), ctx_.get()); }
+    axr_batch* get() const { return batch_.get(); }
+
+private:
+    Context ctx_;
+    std::shared_ptr<axr_batch> batch_;
+};
+
+// Tunes the context's launch form and per-density-class raster parameter on `draws`.
+inline void autotune(const Context& ctx, const std::vector<Draw>& draws, int repeats = 3) {
+    std::vector<axr_draw_desc> d = descs(draws);
+    check(axr_batch_autotune(ctx.get(), d.data(), (int32_t)d.size(), repeats, nullptr), ctx.get());
+}
+
+// ---------------------------------------------------------------- serving loop
+class Server {
+public:
+    explicit Server(const axr_server_config& cfg) {
+        axr_server* s = nullptr;
+        check(axr_server_create(&cfg, &s));
+        srv_.reset(s, axr_server_destroy);
+    }
+    int addTexture(const uint8_t* rgba, int width, int height) {
+        int32_t id = -1;
+        check_(axr_server_add_texture(srv_.get(), rgba, width, height, &id));
+        return id;
+    }
+    int addMesh(const axr_server_mesh_desc& desc) {
+        int32_t id = -1;
+        check_(axr_server_add_mesh(srv_.get(), &desc, &id));
+        return id;
+    }
+    uint64_t submit(const axr_server_request& req) {
+        uint64_t t = 0;
+        check_(axr_server_submit(srv_.get(), &req, &t));
+        return t;
+    }
+    axr_server_result wait(uint64_t ticket, int timeout_ms = -1) {
+        axr_server_result r{};
+        check_(axr_server_wait(srv_.get(), ticket, timeout_ms, &r));
+        return r;
+    }
+    axr_server_stats stats() {
+        axr_server_stats s{};
+        check_(axr_server_get_stats(srv_.get(), &s));
+        return s;
+    }
+    static uint64_t now() { return axr_server_now_ns(); }
+
+private:
+    void check_(axr_status s) {
+        if (s != AXR_OK) throw Error(s, axr_server_last_error(srv_.get()));
+    }
+    std::shared_ptr<axr_server> srv_;
 };
 
 }  // namespace axr

@@ -97,6 +97,13 @@ def make_camera(c) -> Camera:
                   float(c.aspect), (C.c_int32 * 4)(*c.viewport))
 
 
+class Obj(C.Structure):
+    _fields_ = [("num_positions", C.c_uint32), ("positions", C.c_void_p), ("num_uvs", C.c_uint32),
+                ("uvs", C.c_void_p), ("num_normals", C.c_uint32), ("normals", C.c_void_p),
+                ("num_corners", C.c_uint32), ("corners", C.c_void_p), ("num_polygons", C.c_uint32),
+                ("polygon_sizes", C.c_void_p)]
+
+
 class Oracle:
     """One CPU oracle library (kind "port" or "ref")."""
 
@@ -129,6 +136,45 @@ class Oracle:
         self._draw.argtypes = [vp, fp, fp, fp, vp, i32, i32, i32, vp, fp]
         for f in (self._camera, self._clip, self._tri, self._sample, self._shade, self._render, self._draw):
             f.restype = C.c_int
+
+    # -- mesh ingest --------------------------------------------------------------------
+    def obj_ingest(self, parsed: dict):
+        """Port only: de-duplicated vertices (n, 14) and faces (m, 3) of a parsed OBJ
+        model (tests/objfile.parse_obj output)."""
+        if self.kind != "port":
+            raise ValueError("obj_ingest is the port's; the reference loads files (obj_load)")
+        pos = np.ascontiguousarray(parsed["positions"], np.float32)
+        uv = np.ascontiguousarray(parsed["uvs"], np.float32)
+        nrm = np.ascontiguousarray(parsed["normals"], np.float32)
+        cor = np.ascontiguousarray(parsed["corners"], np.int32)
+        sizes = np.ascontiguousarray(parsed["polygon_sizes"], np.uint32)
+        o = Obj(pos.shape[0], pos.ctypes.data, uv.shape[0], uv.ctypes.data, nrm.shape[0], nrm.ctypes.data,
+                cor.shape[0], cor.ctypes.data, sizes.shape[0], sizes.ctypes.data)
+        nc = max(1, cor.shape[0])
+        verts = np.zeros((nc, 14), np.float32)
+        faces = np.zeros((nc, 3), np.uint32)
+        nv, nf = C.c_uint32(), C.c_uint32()
+        f = self.lib.port_obj_ingest
+        f.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p, C.POINTER(C.c_uint32)]
+        f.restype = C.c_int
+        if f(C.addressof(o), verts.ctypes.data, C.byref(nv), faces.ctypes.data, C.byref(nf)) != 0:
+            raise RuntimeError("port_obj_ingest failed")
+        return verts[: nv.value].copy(), faces[: nf.value].copy()
+
+    def obj_load(self, path: str):
+        """Reference only: AR::Mesh(path) -> vertices (n, 14), faces (m, 3), groups (g, 2)."""
+        if self.kind != "ref":
+            raise ValueError("obj_load runs the reference loader")
+        counts = (C.c_uint32 * 3)()
+        self.lib.ref_obj_load.argtypes = [C.c_char_p, C.c_void_p]
+        if self.lib.ref_obj_load(str(path).encode(), counts) != 0:
+            raise RuntimeError("reference Mesh(path) failed")
+        verts = np.zeros((max(1, counts[0]), 14), np.float32)
+        faces = np.zeros((max(1, counts[1]), 3), np.uint32)
+        groups = np.zeros((max(1, counts[2]), 2), np.uint64)
+        self.lib.ref_obj_fetch.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        self.lib.ref_obj_fetch(verts.ctypes.data, faces.ctypes.data, groups.ctypes.data)
+        return verts[: counts[0]], faces[: counts[1]], groups[: counts[2]]
 
     # -- stages -----------------------------------------------------------------------
     def camera(self, cam) -> np.ndarray:

@@ -70,6 +70,25 @@ typedef struct axo_camera {
     int32_t viewport[4]; /* x, y, width, height */
 } axo_camera;
 
+/* A parsed OBJ model before Mesh::parseModelFile's de-duplication (src/mesh.cpp:300-415):
+ * the "v" / "vt" / "vn" pools and, per face line, its corners as 0-based (v, vt, vn)
+ * index triples (vt / vn may be -1 or out of range: absent), corners with an invalid v
+ * dropped. A de-duplicated vertex is 14 floats: position[3], uv[2], normal[3],
+ * tangent[3], bitangent[3]. */
+typedef struct axo_obj {
+    uint32_t num_positions;
+    const float* positions;
+    uint32_t num_uvs;
+    const float* uvs;
+    uint32_t num_normals;
+    const float* normals;
+    uint32_t num_corners;
+    const int32_t* corners;
+    uint32_t num_polygons;
+    const uint32_t* polygon_sizes;
+} axo_obj;
+#define AXO_VERTEX_FLOATS 14
+
 /* ClippedVertex (reference include/pipeline.hpp:13-16) flattened to 18 floats:
  * position[3], uv[2], normal[3], tangent[3], bitangent[3], clipPos[4]. */
 #define AXO_CV_FLOATS 18

@@ -57,6 +57,9 @@ int port_shade(const axo_shader* sh, const axo_material* mat, const float* model
                const float* cam_pos, const float* verts, const float* bar, float* out);
 int port_draw(const axo_mesh* mesh, const float* model, const float* view_proj, const float* cam_pos,
               const axo_shader* shader, int width, int height, int threads, uint8_t* bgra, float* depth);
+/* Vertex de-duplication, fan triangulation and tangent frames of a parsed OBJ model
+ * (ingest.c); verts_out holds num_corners * 14 floats, faces_out num_corners * 3. */
+int port_obj_ingest(const axo_obj* in, float* verts_out, uint32_t* nv_out, uint32_t* faces_out, uint32_t* nf_out);
 int port_render(const axo_mesh* mesh, const float* model, const axo_camera* camera, const axo_shader* shader,
                 int width, int height, int threads, int max_faces_per_draw, uint8_t* bgra, float* depth,
                 float* matrices_out48);

@@ -404,4 +404,45 @@ int ref_draw(const axo_mesh* mesh, const float* model, const float* view_proj, c
     }
 }
 
+// AR::Mesh(path) (src/mesh.cpp:8-27, 300-415, 222-298) on an OBJ file: counts of the
+// loaded mesh, then its vertices (14 floats: position, uv, normal, tangent, bitangent),
+// faces (3 indices) and material groups (start, count) through ref_obj_fetch.
+static std::unique_ptr<AR::Mesh> g_obj_mesh;
+
+int ref_obj_load(const char* path, uint32_t* counts3) {
+    try {
+        g_obj_mesh = std::make_unique<AR::Mesh>(std::string(path));
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "ref_obj_load: reference threw: %s\n", e.what());
+        return 2;
+    }
+    counts3[0] = (uint32_t)g_obj_mesh->getVertices().size();
+    counts3[1] = (uint32_t)g_obj_mesh->getFaces().size();
+    counts3[2] = (uint32_t)g_obj_mesh->getMaterialGroups().size();
+    return 0;
+}
+
+int ref_obj_fetch(float* verts14, uint32_t* faces3, uint64_t* groups2) {
+    if (!g_obj_mesh) return 1;
+    size_t k = 0;
+    for (const AR::Vertex& v : g_obj_mesh->getVertices()) {
+        const float f[14] = {v.position.x, v.position.y, v.position.z, v.uv.x, v.uv.y, v.normal.x, v.normal.y,
+                             v.normal.z, v.tangent.x, v.tangent.y, v.tangent.z, v.bitangent.x, v.bitangent.y,
+                             v.bitangent.z};
+        std::memcpy(verts14 + 14 * k++, f, sizeof(f));
+    }
+    k = 0;
+    for (const AR::Face& f : g_obj_mesh->getFaces()) {
+        for (int j = 0; j < 3; ++j) faces3[3 * k + j] = j < (int)f.vertexIndices.size() ? f.vertexIndices[j] : 0u;
+        ++k;
+    }
+    k = 0;
+    for (const AR::MaterialGroup& g : g_obj_mesh->getMaterialGroups()) {
+        groups2[2 * k] = g.startIndex;
+        groups2[2 * k + 1] = g.faceCount;
+        ++k;
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -7,6 +7,7 @@ stores its inputs (mesh arrays, textures, matrices) next to the reference's outp
 tests on another machine feed exactly the same bytes to the code under test.
 
     python tests/golden/make_golden.py        # rewrites tests/golden/*.npz
+    python tests/golden/make_golden.py obj    # rewrites only the mesh-ingest fixtures
 """
 from __future__ import annotations
 
@@ -74,10 +75,41 @@ def save_scene(path, sc, view_proj, bgra_in, depth_in, bgra, depth):
         bgra_in=bgra_in, depth_in=depth_in, bgra=bgra, depth=depth, **mats)
 
 
+def obj_cases():
+    """OBJ texts for the mesh-ingest fixtures (tests/objfile.py)."""
+    sys.path.insert(0, str(HERE.parent))
+    import objfile
+
+    cases = [("sphere", objfile.sphere_obj(24, 12)), ("sphere_fine", objfile.sphere_obj(96, 48))]
+    cases += [(f"tricky{k}", objfile.tricky_obj(k)) for k in range(3)]
+    return cases
+
+
+def make_obj_goldens(ref):
+    """The reference's Mesh(path) on each OBJ text: vertices (position, uv, normal,
+    tangent, bitangent), faces and material groups, stored with the text."""
+    import tempfile
+
+    for old in HERE.glob("obj_*.npz"):
+        old.unlink()
+    with tempfile.TemporaryDirectory() as d:
+        for name, text in obj_cases():
+            path = Path(d) / f"{name}.obj"
+            path.write_text(text)
+            verts, faces, groups = ref.obj_load(str(path))
+            np.savez_compressed(HERE / f"obj_{name}.npz", text=np.asarray(text), vertices=verts, faces=faces,
+                                groups=groups)
+            print(f"obj_{name:12s} vertices={verts.shape[0]} faces={faces.shape[0]} groups={groups.tolist()}")
+
+
 def main():
     ref = Oracle("ref")
+    if sys.argv[1:] == ["obj"]:
+        make_obj_goldens(ref)
+        return
     for old in HERE.glob("*.npz"):
         old.unlink()
+    make_obj_goldens(ref)
     for i, sc in enumerate(scene_list()):
         vp = ref.camera(sc.camera)[2]
         if sc.name == "sphere_close":

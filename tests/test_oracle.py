@@ -112,3 +112,40 @@ def test_port_draw_into_existing_framebuffer_matches_reference(ref, port):
     bgra = W.noise_texture(sc.width, sc.height, seed=6)
     vp = port.camera(sc.camera)[2]
     assert_parity(port.draw(sc, vp, bgra=bgra, depth=depth), ref.draw(sc, vp, bgra=bgra, depth=depth), "prefilled")
+
+
+# ---------------------------------------------------------------- mesh ingest
+def _obj_goldens():
+    from helpers import GOLDEN
+
+    return sorted(p.stem[len("obj_"):] for p in GOLDEN.glob("obj_*.npz"))
+
+
+@pytest.mark.parametrize("name", _obj_goldens())
+def test_obj_ingest_port_matches_reference_fixture(port, name):
+    """The port's de-duplication, triangulation and tangent frames against the reference's
+    Mesh(path) on the same OBJ text (fixture made by tests/golden/make_golden.py)."""
+    import objfile
+    from helpers import GOLDEN
+
+    z = np.load(GOLDEN / f"obj_{name}.npz")
+    parsed = objfile.parse_obj(str(z["text"]))
+    verts, faces = port.obj_ingest(parsed)
+    assert verts.shape == z["vertices"].shape and faces.shape == z["faces"].shape
+    assert np.array_equal(verts.view(np.uint32), z["vertices"].view(np.uint32))
+    assert np.array_equal(faces, z["faces"])
+    assert np.array_equal(parsed["groups"], z["groups"])
+
+
+def test_obj_ingest_port_matches_reference_live(port, ref, tmp_path):
+    import objfile
+
+    for seed in range(10, 16):
+        text = objfile.tricky_obj(seed)
+        path = tmp_path / f"t{seed}.obj"
+        path.write_text(text)
+        rv, rf, rg = ref.obj_load(str(path))
+        parsed = objfile.parse_obj(text)
+        pv, pf = port.obj_ingest(parsed)
+        assert np.array_equal(pv.view(np.uint32), rv.view(np.uint32)) and np.array_equal(pf, rf)
+        assert np.array_equal(parsed["groups"], rg)
