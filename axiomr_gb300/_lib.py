@@ -67,6 +67,14 @@ class BatchInfo(C.Structure):
                 ("pixels", C.c_uint64), ("tiles", C.c_uint64), ("device_bytes", C.c_uint64)]
 
 
+class ObjDesc(C.Structure):
+    _fields_ = [("num_positions", C.c_uint32), ("positions", C.c_void_p), ("num_uvs", C.c_uint32),
+                ("uvs", C.c_void_p), ("num_normals", C.c_uint32), ("normals", C.c_void_p),
+                ("num_corners", C.c_uint32), ("corners", C.c_void_p), ("num_polygons", C.c_uint32),
+                ("polygon_sizes", C.c_void_p), ("num_groups", C.c_uint32), ("groups", C.c_void_p),
+                ("num_materials", C.c_uint32), ("materials", C.c_void_p)]
+
+
 class Profile(C.Structure):
     _fields_ = [("draws", C.c_uint32), ("pad_", C.c_uint32), ("vertex_ms", C.c_double), ("geometry_ms", C.c_double),
                 ("large_ms", C.c_double), ("scan_ms", C.c_double), ("shade_ms", C.c_double),
@@ -137,6 +145,9 @@ SIGNATURES = {
     "axr_texture_destroy": (None, [P, P]),
     "axr_mesh_create": (S, [P, P, PP]),
     "axr_mesh_update": (S, [P, P, P]),
+    "axr_mesh_create_from_obj": (S, [P, P, PP]),
+    "axr_mesh_read": (S, [P, P, P, P]),
+    "axr_mesh_counts": (S, [P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "axr_mesh_destroy": (None, [P, P]),
     "axr_framebuffer_create": (S, [P, C.c_int32, C.c_int32, PP]),
     "axr_framebuffer_destroy": (None, [P, P]),

@@ -215,7 +215,11 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
                     prop.major, prop.minor);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux.stream, cudaStreamNonBlocking);
+    // the side stream runs work that fills gaps beside the main stream's (the clipped-winner
+    // pass, the batched form's clears): lowest priority, so the main stream's CTAs go first
+    int prio_low = 0, prio_high = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->aux.stream, cudaStreamNonBlocking, prio_low);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, sizeof(DevCounters));

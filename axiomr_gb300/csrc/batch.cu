@@ -8,7 +8,7 @@
 //   2. faces      256-face units in draw order: clip, cull, setup, small-triangle raster;
 //                 large triangles go to one shared list with one item per 16x16 tile
 //   3. large      warps take items of the shared list (4 per atomic), any draw
-//   4. tiles      64-tile units, 8 tiles per warp: a warp reads a 16x16 tile's depth keys,
+//   4. tiles      tile units, one warp per 16x16 tile: a warp reads the tile's depth keys,
 //                 shades the winners (compacted across the warp through shared memory),
 //                 and writes the whole tile once. A draw that asks for a clear gets it
 //                 fused here: the tile is staged in shared memory with the clear colour
@@ -517,8 +517,9 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
     const unsigned dirty = s_dirty;
     const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
     const bool full = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth);
-    // key-less tiles with a full clear: direct stores, spread over the warps
-    if (full) {
+    // key-less tiles with a full clear: direct stores, spread over the warps (unless the
+    // clear kernel has written them already)
+    if (full && !(ui.flags & kBatchClearedApart)) {
         unsigned clean = all & ~dirty;
         for (int k = 0; clean; ++k) {
             const int t = __ffs(clean) - 1;
@@ -572,20 +573,64 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
     if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
+// Clear of both planes of the phased form's fully cleared draws, in spans of kClearUnit
+// pixels of one draw with 16-byte stores (planes are 256-byte aligned and spans start at
+// multiples of 4 pixels). One CTA per SM walks the spans: stores need issue slots, not
+// latency hiding, so one CTA per SM reaches the HBM write rate while leaving the rest of
+// each SM to the vertex, face and large phases it runs beside (on a low-priority side
+// stream); the tile pass waits for it.
+__global__ void __launch_bounds__(kBatchBlock) batch_clear_kernel(const __grid_constant__ BatchParams bp) {
+    const uint2* units = reinterpret_cast<const uint2*>(bp.units) + bp.vert_units + bp.face_units + bp.tile_units;
+    for (uint32_t u = blockIdx.x; u < bp.clear_units; u += gridDim.x) {
+        const uint2 r = __ldg(units + u);
+        const BatchDraw* bd = &bp.draws[r.x];
+        uint32_t* color = bd->p.target.color;
+        float* depth = bd->p.target.depth;
+        const size_t n = (size_t)bd->p.target.width * (size_t)bd->p.target.height;
+        const uint32_t cc = __ldg(&bd->clear_bgra);
+        const float cd = __ldg(&bd->clear_depth);
+        const size_t lo = (size_t)r.y * kClearUnit, hi = min(n, lo + kClearUnit);
+        const uint4 c4 = make_uint4(cc, cc, cc, cc);
+        const float4 d4 = make_float4(cd, cd, cd, cd);
+        const size_t v_hi = lo + ((hi - lo) & ~size_t(3));
+        for (size_t i = lo + 4 * (size_t)threadIdx.x; i < v_hi; i += 4 * (size_t)kBatchBlock) {
+            *reinterpret_cast<uint4*>(color + i) = c4;
+            *reinterpret_cast<float4*>(depth + i) = d4;
+        }
+        for (size_t i = v_hi + threadIdx.x; i < hi; i += kBatchBlock) {
+            color[i] = cc;
+            depth[i] = cd;
+        }
+    }
+}
+
 template <int S>
-cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, cudaEvent_t* ev,
-                           uint64_t* launches) {
+cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, const AuxStream* aux,
+                           cudaEvent_t* ev, uint64_t* launches) {
     cudaError_t e = cudaMemsetAsync(bp.counters, 0, kBatchCountersReset, stream);
     if (e != cudaSuccess) return e;
     if (form == kFormPhased) {
         auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], stream) : cudaSuccess; };
         if ((e = mark(0)) != cudaSuccess) return e;
+        const bool side = bp.clear_units && aux;
+        if (side) {
+            if ((e = cudaEventRecord(aux->fork, stream)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) return e;
+        }
+        if (bp.clear_units) {
+            const unsigned g = min(bp.clear_units, (unsigned)num_sms);
+            batch_clear_kernel<<<g, kBatchBlock, 0, side ? aux->stream : stream>>>(bp);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            *launches += 1;
+        }
+        if (side && (e = cudaEventRecord(aux->join, aux->stream)) != cudaSuccess) return e;
         if (bp.vert_units) batch_vertex_kernel<S><<<bp.vert_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1)) != cudaSuccess) return e;
         if (bp.face_units) batch_face_kernel<<<bp.face_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(2)) != cudaSuccess) return e;
         if (bp.face_units) batch_large_kernel<<<(unsigned)num_sms * 5u, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(3)) != cudaSuccess) return e;
+        if (side && (e = cudaStreamWaitEvent(stream, aux->join, 0)) != cudaSuccess) return e;
         if (bp.tile_units) batch_tile_kernel<S><<<bp.tile_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(4)) != cudaSuccess) return e;
         *launches += (bp.vert_units ? 1 : 0) + (bp.face_units ? 2 : 0) + (bp.tile_units ? 1 : 0);
@@ -625,13 +670,13 @@ cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStr
 }  // namespace
 
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
-                         cudaEvent_t* phase_events, uint64_t* launches) {
+                         const AuxStream* aux, cudaEvent_t* phase_events, uint64_t* launches) {
     switch (shader) {
-        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, phase_events, launches);
-        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, phase_events, launches);
-        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, phase_events, launches);
-        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, phase_events, launches);
-        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches);
+        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, aux, phase_events, launches);
+        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, aux, phase_events, launches);
+        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, aux, phase_events, launches);
+        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, aux, phase_events, launches);
+        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, aux, phase_events, launches);
         default: return cudaErrorInvalidValue;
     }
 }

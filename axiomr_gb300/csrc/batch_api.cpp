@@ -138,6 +138,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         total_units += (drawn ? ceil_div(d.mesh->num_vertices, kVertUnit) : 0u) + ceil_div(d.mesh->num_drawn, kFaceUnit);
         if (drawn || (d.clear_flags & (AXR_DRAW_CLEAR_COLOR | AXR_DRAW_CLEAR_DEPTH)))
             total_units += ceil_div((uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y, tile_unit);
+        if (form == kFormPhased && (d.clear_flags & AXR_DRAW_CLEAR_COLOR) && (d.clear_flags & AXR_DRAW_CLEAR_DEPTH))
+            total_units += ceil_div((uint64_t)d.framebuffer->width * d.framebuffer->height, kClearUnit);
     }
     const size_t table_bytes = align256(sizeof(BatchDraw) * (size_t)std::max(count, 1));
     const size_t units_bytes = align256(sizeof(UnitRef) * std::max<size_t>(total_units, 1));
@@ -168,7 +170,7 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     b->launches.clear();
     for (const auto& g : groups) {
         const size_t first = g.second.first, last = g.second.second, n = last - first;
-        std::vector<UnitRef> uv, uf, ut;
+        std::vector<UnitRef> uv, uf, ut, uc;
         for (size_t k = 0; k < n; ++k) {
             const axr_draw_desc& d = draws[order[first + k]];
             const axr_mesh* m = d.mesh;
@@ -208,11 +210,19 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             for (uint32_t j = 0; j < nv; ++j) uv.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nf; ++j) uf.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nt; ++j) ut.push_back(UnitRef{(uint32_t)k, j});
+            // the phased form clears both planes of a fully cleared draw in its own kernel,
+            // beside the vertex, face and large phases
+            if (form == kFormPhased && (bd.flags & kBatchClearColor) && (bd.flags & kBatchClearDepth)) {
+                bd.flags |= kBatchClearedApart;
+                const uint32_t nc = ceil_div((uint64_t)fb->width * fb->height, kClearUnit);
+                for (uint32_t j = 0; j < nc; ++j) uc.push_back(UnitRef{(uint32_t)k, j});
+            }
         }
         const size_t unit_at = units.size();
         units.insert(units.end(), uv.begin(), uv.end());
         units.insert(units.end(), uf.begin(), uf.end());
         units.insert(units.end(), ut.begin(), ut.end());
+        units.insert(units.end(), uc.begin(), uc.end());
         axr_batch::Launch L{};
         L.shader = g.first;
         BatchParams& bp = L.params;
@@ -226,6 +236,7 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         bp.vert_units = (uint32_t)uv.size();
         bp.face_units = (uint32_t)uf.size();
         bp.tile_units = (uint32_t)ut.size();
+        bp.clear_units = (uint32_t)uc.size();
         bp.large_cap = large_cap;
         bp.item_cap = item_cap;
         bp.tiles_per_warp = tiles_per_warp;
@@ -268,7 +279,7 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
             ev = &ctx->batch_events[ctx->batch_events_used];
             ctx->batch_events_used += 5;
         }
-        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, ctx->stream, ev, &ctx->launches));
+        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, ctx->stream, &ctx->aux, ev, &ctx->launches));
     }
     return AXR_OK;
 }

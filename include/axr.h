@@ -128,6 +128,39 @@ typedef struct axr_mesh_desc {
     const axr_material_desc* materials;
 } axr_mesh_desc;
 
+/* The mesh of an OBJ model parsed on the host, de-duplicated, triangulated and given its
+ * tangent frames on the device: Mesh::parseModelFile after its text parsing
+ * (src/mesh.cpp:300-415) and Mesh::calculateTangentBitangent (src/mesh.cpp:222-298).
+ * Corners are the face lines' corners in file order as 0-based (v, vt, vn) triples, vt /
+ * vn -1 (or out of range) when absent or not yet defined at that line, corners with an
+ * invalid v dropped (as the reference parser skips them); polygon_sizes gives each face
+ * line's corner count (a polygon of n >= 3 corners becomes the fan of n-2 triangles);
+ * groups count triangulated faces. The result equals what the reference's Mesh holds
+ * (vertices in order of first appearance, bit for bit). */
+typedef struct axr_obj_desc {
+    uint32_t num_positions;
+    const float* positions;  /* "v": 3 per entry */
+    uint32_t num_uvs;
+    const float* uvs;        /* "vt": 2 per entry */
+    uint32_t num_normals;
+    const float* normals;    /* "vn": 3 per entry */
+    uint32_t num_corners;
+    const int32_t* corners;  /* 3 per corner */
+    uint32_t num_polygons;
+    const uint32_t* polygon_sizes;
+    uint32_t num_groups;
+    const axr_group_desc* groups;
+    uint32_t num_materials;
+    const axr_material_desc* materials;
+} axr_obj_desc;
+axr_status axr_mesh_create_from_obj(axr_context* ctx, const axr_obj_desc* obj, axr_mesh** out);
+/* A mesh's vertices back on the host as 14 floats each (position, uv, normal, tangent,
+ * bitangent; zeros for absent arrays) and/or its faces as 3 indices each; either may be
+ * NULL. Blocks. */
+axr_status axr_mesh_read(axr_context* ctx, const axr_mesh* mesh, float* vertices14, uint32_t* indices3);
+/* Counts of a mesh (any argument NULL to skip). */
+axr_status axr_mesh_counts(const axr_mesh* mesh, uint32_t* vertices, uint32_t* faces, uint32_t* drawn);
+
 /* Upload a mesh (host pointers; the call returns after the data has been copied). */
 axr_status axr_mesh_create(axr_context* ctx, const axr_mesh_desc* desc, axr_mesh** out);
 /* Re-upload vertex attributes and indices of an existing mesh with the same counts,

@@ -12,6 +12,16 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 COLOR_TOLERANCE_LSB = 1
 
 
+def same_bits(a, b) -> bool:
+    """Float arrays equal bit for bit, except that any NaN matches any NaN: the bit pattern
+    of a NaN that an operation creates is the machine's default NaN (x86, Arm and the GPU
+    differ), and the reference makes NaNs on degenerate input (a tangent frame of a
+    zero-area triangle)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    return a.shape == b.shape and bool(np.all((a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))))
+
+
 def golden_names():
     return sorted(p.stem[len("scene_"):] for p in GOLDEN.glob("scene_*.npz"))
 

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from axiomr_gb300 import workloads as W
-from helpers import GOLDEN, assert_parity, golden_names, load_golden
+from helpers import GOLDEN, assert_parity, golden_names, load_golden, same_bits
 
 X86 = platform.machine() in ("x86_64", "AMD64")
 
@@ -16,10 +16,6 @@ def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
 
 
-def same_bits(a, b):
-    a = np.asarray(a, np.float32)
-    b = np.asarray(b, np.float32)
-    return a.shape == b.shape and bool(np.all((bits(a) == bits(b)) | (np.isnan(a) & np.isnan(b))))
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -132,7 +128,7 @@ def test_obj_ingest_port_matches_reference_fixture(port, name):
     parsed = objfile.parse_obj(str(z["text"]))
     verts, faces = port.obj_ingest(parsed)
     assert verts.shape == z["vertices"].shape and faces.shape == z["faces"].shape
-    assert np.array_equal(verts.view(np.uint32), z["vertices"].view(np.uint32))
+    assert same_bits(verts, z["vertices"])
     assert np.array_equal(faces, z["faces"])
     assert np.array_equal(parsed["groups"], z["groups"])
 
@@ -147,5 +143,5 @@ def test_obj_ingest_port_matches_reference_live(port, ref, tmp_path):
         rv, rf, rg = ref.obj_load(str(path))
         parsed = objfile.parse_obj(text)
         pv, pf = port.obj_ingest(parsed)
-        assert np.array_equal(pv.view(np.uint32), rv.view(np.uint32)) and np.array_equal(pf, rf)
+        assert same_bits(pv, rv) and np.array_equal(pf, rf)
         assert np.array_equal(parsed["groups"], rg)
