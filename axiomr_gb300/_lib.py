@@ -80,7 +80,21 @@ class Profile(C.Structure):
                 ("large_ms", C.c_double), ("scan_ms", C.c_double), ("shade_ms", C.c_double),
                 ("clipped_ms", C.c_double), ("kernel_launches", C.c_uint64), ("batch_launches", C.c_uint64),
                 ("batch_vertex_ms", C.c_double), ("batch_face_ms", C.c_double), ("batch_large_ms", C.c_double),
-                ("batch_tile_ms", C.c_double)]
+                ("batch_tile_ms", C.c_double), ("batch_clear_ms", C.c_double)]
+
+
+class CameraState(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("orientation", C.c_float * 4), ("forward", C.c_float * 3),
+                ("right", C.c_float * 3), ("up", C.c_float * 3), ("delta_yaw", C.c_float), ("delta_pitch", C.c_float),
+                ("velocity", C.c_float * 3), ("fov_degrees", C.c_float), ("aspect_ratio", C.c_float),
+                ("near_plane", C.c_float), ("far_plane", C.c_float), ("movement_speed", C.c_float),
+                ("mouse_sensitivity", C.c_float), ("last_mouse", C.c_float * 2), ("viewport", C.c_int32 * 4),
+                ("view", C.c_float * 16), ("projection", C.c_float * 16), ("view_proj", C.c_float * 16),
+                ("view_dirty", C.c_int32), ("projection_dirty", C.c_int32)]
+
+
+class InputState(C.Structure):
+    _fields_ = [("mouse", C.c_float * 2), ("mouse_buttons", C.c_uint8 * 3), ("keys", C.c_uint8 * 256)]
 
 
 class DrawStats(C.Structure):
@@ -157,8 +171,29 @@ SIGNATURES = {
     "axr_framebuffer_read_async": (S, [P, P, P, P]),
     "axr_framebuffer_write": (S, [P, P, P, P]),
     "axr_framebuffers_read_async": (S, [P, C.c_int32, P, P, P]),
+    "axr_readback_create": (S, [P, PP]),
+    "axr_readback_destroy": (None, [P, P]),
+    "axr_readback_start": (S, [P, P, C.c_int32, P, P, P]),
+    "axr_readback_wait": (S, [P, P]),
     "axr_framebuffer_size": (S, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "axr_framebuffer_device_pointers": (S, [P, PP, PP]),
+    "axr_camera_init": (S, [P, P, P, C.c_float, C.c_float]),
+    "axr_camera_set_position": (S, [P, P]),
+    "axr_camera_set_target": (S, [P, P]),
+    "axr_camera_set_fov": (S, [P, C.c_float]),
+    "axr_camera_set_aspect_ratio": (S, [P, C.c_float]),
+    "axr_camera_set_viewport": (S, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "axr_camera_handle_input": (S, [P, P]),
+    "axr_camera_update": (S, [P, C.c_float]),
+    "axr_camera_describe": (S, [P, P]),
+    "axr_png_bound": (C.c_uint64, [C.c_uint32, C.c_uint32, C.c_uint32]),
+    "axr_framebuffers_encode_png": (S, [P, C.c_int32, P, C.c_uint32, P, P, P]),
+    "axr_framebuffers_read_png": (S, [P, C.c_int32, P, C.c_uint32, P, P, P]),
+    "axr_png_batch_create": (S, [P, PP]),
+    "axr_png_batch_destroy": (None, [P, P]),
+    "axr_png_batch_encode": (S, [P, P, C.c_int32, P, C.c_uint32]),
+    "axr_png_batch_sizes": (S, [P, P, P]),
+    "axr_png_batch_read": (S, [P, P, P, P]),
     "axr_set_shader": (S, [P, P]),
     "axr_set_camera": (S, [P, P]),
     "axr_set_framebuffer": (S, [P, P]),

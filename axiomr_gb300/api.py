@@ -78,7 +78,7 @@ class Context:
                 "clipped_ms": pr.clipped_ms, "kernel_launches": pr.kernel_launches,
                 "batch_launches": pr.batch_launches, "batch_vertex_ms": pr.batch_vertex_ms,
                 "batch_face_ms": pr.batch_face_ms, "batch_large_ms": pr.batch_large_ms,
-                "batch_tile_ms": pr.batch_tile_ms}
+                "batch_tile_ms": pr.batch_tile_ms, "batch_clear_ms": pr.batch_clear_ms}
 
     def fp32_peak_tflops(self) -> float:
         """FP32 issue peak of the device, measured with independent FMA chains."""
@@ -270,6 +270,10 @@ class Framebuffer:
               self.ctx.handle)
         return bgra, depth
 
+    def read_png(self, channels: int = 3) -> bytes:
+        """The colour plane as a PNG file (top row first; RGB8 or RGBA8), encoded on the GPU."""
+        return read_png(self.ctx, [self], channels)[0]
+
     def write(self, bgra: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None) -> None:
         b = None if bgra is None else np.ascontiguousarray(bgra, np.uint8)
         d = None if depth is None else np.ascontiguousarray(depth, np.float32)
@@ -288,25 +292,26 @@ class Framebuffer:
 
 
 class Camera:
-    """Camera(position, target, fov, aspect) + update(0) (src/camera.cpp:30-100)."""
+    """The reference Camera (include/camera.hpp:6-67, src/camera.cpp:30-205) on the
+    library's axr_camera_state: setPosition, setTarget, setFov, setAspectRatio,
+    setViewport, handleInput and update(deltaTime) behave as the reference's. The
+    constructor also runs update(0), as a frame loop does before its first draw (the
+    reference constructor leaves the view matrix at identity until an update); pass
+    update=False for the bare constructor."""
 
     def __init__(self, position=(0.0, 0.0, 0.0), target=(0.0, 0.0, -1.0), fov: float = 60.0,
-                 aspect: float = 16.0 / 9.0, viewport=(0, 0, 800, 600)):
-        self.position = tuple(float(v) for v in position)
+                 aspect: float = 16.0 / 9.0, viewport=(0, 0, 800, 600), update: bool = True):
+        self._lib = _lib.load()
+        self.state = _lib.CameraState()
         self.target = tuple(float(v) for v in target)
         self.fov = float(fov)
         self.aspect = float(aspect)
-        self.viewport = tuple(int(v) for v in viewport)
-        lib = _lib.load()
-        self.view = np.zeros(16, np.float32)
-        self.projection = np.zeros(16, np.float32)
-        self.view_proj = np.zeros(16, np.float32)
-        pos = _f32(self.position)
-        tgt = _f32(self.target)
-        check(lib.axr_camera_matrices(pos.ctypes.data, tgt.ctypes.data, self.fov, self.aspect, self.view.ctypes.data,
-                                      self.projection.ctypes.data, self.view_proj.ctypes.data))
-        self.viewport_matrix = np.zeros(16, np.float32)
-        check(lib.axr_viewport_matrix(*self.viewport, self.viewport_matrix.ctypes.data))
+        pos, tgt = _f32(position), _f32(target)
+        check(self._lib.axr_camera_init(C.byref(self.state), pos.ctypes.data, tgt.ctypes.data, self.fov, self.aspect))
+        self.setViewport(*viewport)
+        self._fixed = None
+        if update:
+            self.update(0.0)
 
     @classmethod
     def from_workload(cls, cam):
@@ -316,20 +321,75 @@ class Camera:
     def from_matrices(cls, view_proj, position, viewport=(0, 0, 1, 1)):
         """A camera with a given view-projection matrix (16 floats, column-major) and eye
         position, e.g. matrices computed elsewhere."""
-        cam = cls.__new__(cls)
-        cam.position = tuple(float(v) for v in position)
-        cam.target = None
-        cam.fov = cam.aspect = None
-        cam.viewport = tuple(int(v) for v in viewport)
-        cam.view = cam.projection = None
-        cam.view_proj = _f32(view_proj).reshape(16).copy()
-        cam.viewport_matrix = np.zeros(16, np.float32)
-        check(_lib.load().axr_viewport_matrix(*cam.viewport, cam.viewport_matrix.ctypes.data))
+        cam = cls(position, (float(position[0]), float(position[1]), float(position[2]) - 1.0), viewport=viewport,
+                  update=False)
+        cam._fixed = _f32(view_proj).reshape(16).copy()
         return cam
 
+    # the reference's setters and motion
+    def setPosition(self, position) -> None:
+        p = _f32(position)
+        check(self._lib.axr_camera_set_position(C.byref(self.state), p.ctypes.data))
+
+    def setTarget(self, target) -> None:
+        t = _f32(target)
+        check(self._lib.axr_camera_set_target(C.byref(self.state), t.ctypes.data))
+
+    def setFov(self, fov: float) -> None:
+        check(self._lib.axr_camera_set_fov(C.byref(self.state), float(fov)))
+
+    def setAspectRatio(self, aspect: float) -> None:
+        check(self._lib.axr_camera_set_aspect_ratio(C.byref(self.state), float(aspect)))
+
+    def setViewport(self, x: int, y: int, width: int, height: int) -> None:
+        check(self._lib.axr_camera_set_viewport(C.byref(self.state), int(x), int(y), int(width), int(height)))
+
+    def handleInput(self, mouse=(0.0, 0.0), right_button: bool = False, keys: str = "") -> None:
+        """Camera::handleInput with the window's mouse position, right-button state and the
+        keys held down (characters, e.g. "WD")."""
+        s = _lib.InputState()
+        s.mouse[0], s.mouse[1] = float(mouse[0]), float(mouse[1])
+        s.mouse_buttons[1] = 1 if right_button else 0
+        for k in keys:
+            s.keys[ord(k) & 255] = 1
+        check(self._lib.axr_camera_handle_input(C.byref(self.state), C.byref(s)))
+
+    def update(self, delta_time: float) -> None:
+        check(self._lib.axr_camera_update(C.byref(self.state), float(delta_time)))
+
+    # accessors
+    @property
+    def position(self) -> tuple:
+        return tuple(float(v) for v in self.state.position)
+
+    @property
+    def viewport(self) -> tuple:
+        return tuple(int(v) for v in self.state.viewport)
+
+    @property
+    def view(self) -> np.ndarray:
+        return np.array(self.state.view, np.float32)
+
+    @property
+    def projection(self) -> np.ndarray:
+        return np.array(self.state.projection, np.float32)
+
+    @property
+    def view_proj(self) -> np.ndarray:
+        return self._fixed.copy() if self._fixed is not None else np.array(self.state.view_proj, np.float32)
+
+    @property
+    def viewport_matrix(self) -> np.ndarray:
+        d = CameraDesc()
+        check(self._lib.axr_camera_describe(C.byref(self.state), C.byref(d)))
+        return np.array(d.viewport, np.float32)
+
     def desc(self) -> CameraDesc:
-        return CameraDesc((C.c_float * 16)(*self.view_proj), (C.c_float * 16)(*self.viewport_matrix),
-                          (C.c_float * 3)(*self.position))
+        d = CameraDesc()
+        check(self._lib.axr_camera_describe(C.byref(self.state), C.byref(d)))
+        if self._fixed is not None:
+            d.view_proj = (C.c_float * 16)(*self._fixed)
+        return d
 
 
 @dataclasses.dataclass
@@ -512,8 +572,18 @@ class Batch:
             pass
 
 
-def draw_batch(ctx: Context, draws: Sequence[Draw]) -> None:
-    """One-shot batch (axr_draw_batch)."""
+def draw_table(draws: Sequence[Draw]):
+    """The draws as the C array of axr_draw_desc that axr_draw_batch takes (built once; a
+    host program keeps such a table and edits cameras or model matrices in place)."""
+    return _draw_descs(draws)
+
+
+def draw_batch(ctx: Context, draws) -> None:
+    """One-shot batch (axr_draw_batch): the draw list is planned and its table uploaded on
+    every call. `draws`: Draw objects, or a table from draw_table()."""
+    if isinstance(draws, C.Array):
+        check(ctx.lib.axr_draw_batch(ctx.handle, draws, len(draws)), ctx.handle)
+        return
     check(ctx.lib.axr_draw_batch(ctx.handle, _draw_descs(draws), len(draws)), ctx.handle)
 
 
@@ -677,6 +747,75 @@ class Server:
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.lib.axr_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def png_bound(width: int, height: int, channels: int = 3) -> int:
+    """Worst-case PNG file size of a width x height framebuffer (axr_png_bound)."""
+    return int(_lib.load().axr_png_bound(width, height, channels))
+
+
+def read_png(ctx: "Context", framebuffers, channels: int = 3) -> list:
+    """PNG files of many framebuffers, encoded by one set of launches and copied back
+    (axr_framebuffers_read_png)."""
+    n = len(framebuffers)
+    if n == 0:
+        return []
+    fbs = (C.c_void_p * n)(*[fb.handle for fb in framebuffers])
+    sizes = (C.c_uint64 * n)()
+    bufs = [np.empty(png_bound(fb.width, fb.height, channels), np.uint8) for fb in framebuffers]
+    ptrs = (C.c_void_p * n)(*[b.ctypes.data for b in bufs])
+    caps = (C.c_uint64 * n)(*[b.nbytes for b in bufs])
+    check(ctx.lib.axr_framebuffers_read_png(ctx.handle, n, fbs, channels, ptrs, caps, sizes), ctx.handle)
+    return [bufs[i][: int(sizes[i])].tobytes() for i in range(n)]
+
+
+class PngBatch:
+    """Pipelined PNG read-back (axr_png_batch_*): encode() enqueues the encode of a list of
+    framebuffers and returns at once; read() waits for it and copies the files to host
+    memory on the batch's own streams, so a caller can render and encode the next frames
+    while the previous ones come back."""
+
+    def __init__(self, ctx: "Context"):
+        self.ctx = ctx
+        self.handle = C.c_void_p()
+        check(ctx.lib.axr_png_batch_create(ctx.handle, C.byref(self.handle)), ctx.handle)
+        self.count = 0
+
+    def encode(self, framebuffers, channels: int = 3) -> None:
+        """framebuffers: Framebuffer objects, or a ctypes array of their handles."""
+        n = len(framebuffers)
+        self._fbs = framebuffers if isinstance(framebuffers, C.Array) else \
+            (C.c_void_p * max(1, n))(*[fb.handle for fb in framebuffers])
+        check(self.ctx.lib.axr_png_batch_encode(self.ctx.handle, self.handle, n, self._fbs, channels), self.ctx.handle)
+        self.count = n
+
+    def sizes(self) -> list:
+        out = (C.c_uint64 * max(1, self.count))()
+        check(self.ctx.lib.axr_png_batch_sizes(self.ctx.handle, self.handle, out), self.ctx.handle)
+        return [int(out[i]) for i in range(self.count)]
+
+    def read_into(self, ptrs, capacities) -> None:
+        """Copy the files to host buffers given as ctypes arrays of pointers and sizes."""
+        check(self.ctx.lib.axr_png_batch_read(self.ctx.handle, self.handle, ptrs, capacities), self.ctx.handle)
+
+    def read(self) -> list:
+        sizes = self.sizes()
+        bufs = [np.empty(max(1, k), np.uint8) for k in sizes]
+        ptrs = (C.c_void_p * max(1, self.count))(*[b.ctypes.data for b in bufs])
+        caps = (C.c_uint64 * max(1, self.count))(*[b.nbytes for b in bufs])
+        self.read_into(ptrs, caps)
+        return [b[:k].tobytes() for b, k in zip(bufs, sizes)]
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.axr_png_batch_destroy(self.ctx.handle, self.handle)
             self.handle = None
 
     def __del__(self):

@@ -261,11 +261,13 @@ void axr_context_destroy(axr_context* ctx) {
     for (cudaEvent_t ev : ctx->batch_events) cudaEventDestroy(ev);
     if (ctx->oneshot) {
         free_batch(ctx->oneshot);
+        free_batch_staging(ctx->oneshot);
         delete ctx->oneshot;
     }
     dfree(ctx->counters);
     dfree(ctx->batch_prof);
     free_scratch(ctx);
+    free_png(ctx);
     if (ctx->aux.stream) cudaStreamSynchronize(ctx->aux.stream);
     if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
     for (int k = 0; k < axr_context::kCopyStreams; ++k) {
@@ -578,6 +580,87 @@ axr_status axr_framebuffer_read_async(axr_context* ctx, const axr_framebuffer* f
     return fb_read(ctx, fb, bgra, depth, false);
 }
 
+}  // extern "C"
+
+// A read-back on its own copy streams: started after the work already on the context
+// stream, but later work on the context stream does not wait for it.
+struct axr_readback {
+    int device = 0;
+    static constexpr int kStreams = 4;
+    cudaStream_t copy[kStreams] = {};
+    cudaEvent_t copied[kStreams] = {};
+    cudaEvent_t ready = nullptr;  // the framebuffers are final (context stream)
+};
+
+namespace {
+
+void release_readback(axr_readback* rb) {
+    for (int k = 0; k < axr_readback::kStreams; ++k) {
+        if (rb->copy[k]) {
+            cudaStreamSynchronize(rb->copy[k]);
+            cudaStreamDestroy(rb->copy[k]);
+        }
+        if (rb->copied[k]) cudaEventDestroy(rb->copied[k]);
+    }
+    if (rb->ready) cudaEventDestroy(rb->ready);
+    delete rb;
+}
+
+}  // namespace
+
+extern "C" {
+
+axr_status axr_readback_create(axr_context* ctx, axr_readback** out) {
+    if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    DeviceGuard g(ctx->device);
+    auto* rb = new axr_readback();
+    rb->device = ctx->device;
+    cudaError_t e = cudaEventCreateWithFlags(&rb->ready, cudaEventDisableTiming);
+    for (int k = 0; e == cudaSuccess && k < axr_readback::kStreams; ++k) {
+        e = cudaStreamCreateWithFlags(&rb->copy[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&rb->copied[k], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        release_readback(rb);
+        return cuda_fail(ctx, e, "read-back streams");
+    }
+    *out = rb;
+    return AXR_OK;
+}
+
+void axr_readback_destroy(axr_context* ctx, axr_readback* rb) {
+    if (!rb) return;
+    DeviceGuard g(rb->device);
+    release_readback(rb);
+}
+
+axr_status axr_readback_start(axr_context* ctx, axr_readback* rb, int32_t count, const axr_framebuffer* const* fbs,
+                              uint8_t* const* bgra, float* const* depth) {
+    if (!ctx || !rb || count < 0 || (count > 0 && !fbs)) return fail(ctx, AXR_E_INVALID, "bad read-back arguments");
+    if (rb->device != ctx->device) return fail(ctx, AXR_E_INVALID, "the read-back belongs to another device");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    AXR_CUDA(ctx, cudaEventRecord(rb->ready, ctx->stream));
+    for (int k = 0; k < axr_readback::kStreams; ++k) AXR_CUDA(ctx, cudaStreamWaitEvent(rb->copy[k], rb->ready, 0));
+    for (int32_t i = 0; i < count; ++i) {
+        const axr_framebuffer* fb = fbs[i];
+        if (!fb) return fail(ctx, AXR_E_INVALID, "framebuffer %d is NULL", i);
+        const size_t n = (size_t)fb->width * fb->height;
+        cudaStream_t st = rb->copy[i % axr_readback::kStreams];
+        if (bgra && bgra[i]) AXR_CUDA(ctx, cudaMemcpyAsync(bgra[i], fb->color, n * 4, cudaMemcpyDeviceToHost, st));
+        if (depth && depth[i]) AXR_CUDA(ctx, cudaMemcpyAsync(depth[i], fb->depth, n * 4, cudaMemcpyDeviceToHost, st));
+    }
+    for (int k = 0; k < axr_readback::kStreams; ++k) AXR_CUDA(ctx, cudaEventRecord(rb->copied[k], rb->copy[k]));
+    return AXR_OK;
+}
+
+axr_status axr_readback_wait(axr_context* ctx, axr_readback* rb) {
+    if (!rb) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    DeviceGuard g(rb->device);
+    for (int k = 0; k < axr_readback::kStreams; ++k) AXR_CUDA(ctx, cudaEventSynchronize(rb->copied[k]));
+    return AXR_OK;
+}
+
 axr_status axr_framebuffer_write(axr_context* ctx, axr_framebuffer* fb, const uint8_t* bgra, const float* depth) {
     if (!ctx || !fb) return fail(ctx, AXR_E_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -784,9 +867,10 @@ axr_status axr_profile_read(axr_context* ctx, axr_profile* out) {
     r.batch_face_ms = bp.phase_ns[1] * 1e-6;
     r.batch_large_ms = bp.phase_ns[2] * 1e-6;
     r.batch_tile_ms = bp.phase_ns[3] * 1e-6;
-    for (size_t k = 0; k + 5 <= ctx->batch_events_used; k += 5) {
-        double* out[4] = {&r.batch_vertex_ms, &r.batch_face_ms, &r.batch_large_ms, &r.batch_tile_ms};
-        for (int j = 0; j < 4; ++j) {
+    for (size_t k = 0; k + 6 <= ctx->batch_events_used; k += 6) {
+        double* out[5] = {&r.batch_clear_ms, &r.batch_vertex_ms, &r.batch_face_ms, &r.batch_large_ms,
+                          &r.batch_tile_ms};
+        for (int j = 0; j < 5; ++j) {
             float ms = 0.f;
             AXR_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->batch_events[k + j], ctx->batch_events[k + j + 1]));
             *out[j] += ms;

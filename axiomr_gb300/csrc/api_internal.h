@@ -20,10 +20,14 @@ void encode_framebuffer_maps(axr_framebuffer* fb);
 void mesh_bounds(const float* pos, uint32_t n, float center[3], float* radius);
 // Release a batch's device memory (the caller synchronises first).
 void free_batch(axr_batch* b);
+// Release a batch's pinned staging and its events (the caller synchronises first).
+void free_batch_staging(axr_batch* b);
 // Plan `count` draws into `b` / launch a planned batch on the context stream (the caller
 // holds ctx->mu; axr_batch_create / axr_batch_launch without the locking).
 axr_status batch_plan(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch* b, bool async);
 axr_status batch_launch(axr_context* ctx, const axr_batch* b);
+// Release the PNG encoder's scratch (the caller synchronises first).
+void free_png(axr_context* ctx);
 
 template <class T>
 cudaError_t dmalloc(T** p, size_t count) {

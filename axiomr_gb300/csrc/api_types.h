@@ -14,6 +14,10 @@
 #include "hostmath.h"
 #include "kernels.h"
 
+namespace axr_internal {
+struct PngState;  // scratch of the PNG encoder (encode.cu)
+}
+
 using axr::DevCounters;
 using axr::DevGroup;
 using axr::DevMaterial;
@@ -70,6 +74,12 @@ struct axr_batch {
     int form = 0;  // axr::kForm*
     uint32_t count = 0;
     uint64_t vertices = 0, faces = 0, pixels = 0, tiles = 0;
+    // pinned staging of the draw and unit tables for uploads on the context stream; two,
+    // used in turn, so that planning the next batch does not wait for the last upload
+    void* stage[2] = {};
+    size_t stage_bytes[2] = {};
+    cudaEvent_t stage_done[2] = {};
+    int stage_next = 0;
 };
 
 struct axr_graph {
@@ -114,13 +124,14 @@ struct axr_context {
     axr_batch* oneshot = nullptr;
     axr::BatchProfile* batch_prof = nullptr;  // device-side phase timing of persistent launches
     int batch_form = axr::kFormPhased;        // launch form of batches planned next
-    std::vector<cudaEvent_t> batch_events;     // phase events of phased launches (5 per launch)
+    std::vector<cudaEvent_t> batch_events;     // phase events of phased launches (6 per launch)
     size_t batch_events_used = 0;
     // profiling: per-draw stage events (4 per draw), reused across reads
     bool profile = false;
     std::vector<cudaEvent_t> event_pool;
     size_t events_used = 0;
     uint64_t launches = 0;
+    axr_internal::PngState* png = nullptr;
 };
 
 namespace axr {

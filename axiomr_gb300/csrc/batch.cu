@@ -575,10 +575,8 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
 
 // Clear of both planes of the phased form's fully cleared draws, in spans of kClearUnit
 // pixels of one draw with 16-byte stores (planes are 256-byte aligned and spans start at
-// multiples of 4 pixels). One CTA per SM walks the spans: stores need issue slots, not
-// latency hiding, so one CTA per SM reaches the HBM write rate while leaving the rest of
-// each SM to the vertex, face and large phases it runs beside (on a low-priority side
-// stream); the tile pass waits for it.
+// multiples of 4 pixels). One CTA per SM walks the spans: 16-byte stores from 256 threads
+// per SM reach the HBM write rate.
 __global__ void __launch_bounds__(kBatchBlock) batch_clear_kernel(const __grid_constant__ BatchParams bp) {
     const uint2* units = reinterpret_cast<const uint2*>(bp.units) + bp.vert_units + bp.face_units + bp.tile_units;
     for (uint32_t u = blockIdx.x; u < bp.clear_units; u += gridDim.x) {
@@ -605,34 +603,30 @@ __global__ void __launch_bounds__(kBatchBlock) batch_clear_kernel(const __grid_c
 }
 
 template <int S>
-cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, const AuxStream* aux,
-                           cudaEvent_t* ev, uint64_t* launches) {
+cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, cudaEvent_t* ev,
+                           uint64_t* launches) {
     cudaError_t e = cudaMemsetAsync(bp.counters, 0, kBatchCountersReset, stream);
     if (e != cudaSuccess) return e;
     if (form == kFormPhased) {
         auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], stream) : cudaSuccess; };
         if ((e = mark(0)) != cudaSuccess) return e;
-        const bool side = bp.clear_units && aux;
-        if (side) {
-            if ((e = cudaEventRecord(aux->fork, stream)) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) return e;
-        }
         if (bp.clear_units) {
+            // at the HBM write rate; running it beside the vertex and face phases (a side
+            // stream) measured no faster, since their key atomics then wait on its writes
             const unsigned g = min(bp.clear_units, (unsigned)num_sms);
-            batch_clear_kernel<<<g, kBatchBlock, 0, side ? aux->stream : stream>>>(bp);
+            batch_clear_kernel<<<g, kBatchBlock, 0, stream>>>(bp);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             *launches += 1;
         }
-        if (side && (e = cudaEventRecord(aux->join, aux->stream)) != cudaSuccess) return e;
+        if ((e = mark(1)) != cudaSuccess) return e;
         if (bp.vert_units) batch_vertex_kernel<S><<<bp.vert_units, kBatchBlock, 0, stream>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1)) != cudaSuccess) return e;
-        if (bp.face_units) batch_face_kernel<<<bp.face_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(2)) != cudaSuccess) return e;
-        if (bp.face_units) batch_large_kernel<<<(unsigned)num_sms * 5u, kBatchBlock, 0, stream>>>(bp);
+        if (bp.face_units) batch_face_kernel<<<bp.face_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(3)) != cudaSuccess) return e;
-        if (side && (e = cudaStreamWaitEvent(stream, aux->join, 0)) != cudaSuccess) return e;
-        if (bp.tile_units) batch_tile_kernel<S><<<bp.tile_units, kBatchBlock, 0, stream>>>(bp);
+        if (bp.face_units) batch_large_kernel<<<(unsigned)num_sms * 5u, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(4)) != cudaSuccess) return e;
+        if (bp.tile_units) batch_tile_kernel<S><<<bp.tile_units, kBatchBlock, 0, stream>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(5)) != cudaSuccess) return e;
         *launches += (bp.vert_units ? 1 : 0) + (bp.face_units ? 2 : 0) + (bp.tile_units ? 1 : 0);
         return cudaSuccess;
     }
@@ -670,13 +664,13 @@ cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStr
 }  // namespace
 
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
-                         const AuxStream* aux, cudaEvent_t* phase_events, uint64_t* launches) {
+                         cudaEvent_t* phase_events, uint64_t* launches) {
     switch (shader) {
-        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, aux, phase_events, launches);
-        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, aux, phase_events, launches);
-        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, aux, phase_events, launches);
-        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, aux, phase_events, launches);
-        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, aux, phase_events, launches);
+        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, phase_events, launches);
+        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, phase_events, launches);
+        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, phase_events, launches);
+        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, phase_events, launches);
+        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -10,12 +10,11 @@ namespace axr {
 
 // Resets the work counters and grid-barrier words, then launches the batch's draws (all
 // of shader kind `shader`) in launch form `form`: kFormPersistent, one cooperative grid of
-// (resident CTAs per SM) x num_sms CTAs running the four phases; kFormPhased, four
-// launches plus, for fully cleared draws, a clear kernel on the side stream of `aux`
-// (forked before the vertex phase, joined before the tile pass; on `stream` itself when
-// aux is NULL). `phase_events` (optional, 5 events, phased form only) are recorded around
-// the four phase launches. Adds the number of kernels launched to *launches.
+// (resident CTAs per SM) x num_sms CTAs running the four phases; kFormPhased, a clear
+// kernel for the fully cleared draws and then four launches. `phase_events` (optional,
+// 6 events, phased form only) are recorded around the five launches. Adds the number of
+// kernels launched to *launches.
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
-                         const AuxStream* aux, cudaEvent_t* phase_events, uint64_t* launches);
+                         cudaEvent_t* phase_events, uint64_t* launches);
 
 }  // namespace axr

@@ -210,8 +210,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             for (uint32_t j = 0; j < nv; ++j) uv.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nf; ++j) uf.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nt; ++j) ut.push_back(UnitRef{(uint32_t)k, j});
-            // the phased form clears both planes of a fully cleared draw in its own kernel,
-            // beside the vertex, face and large phases
+            // the phased form clears both planes of a fully cleared draw in its own kernel
+            // before the other phases
             if (form == kFormPhased && (bd.flags & kBatchClearColor) && (bd.flags & kBatchClearDepth)) {
                 bd.flags |= kBatchClearedApart;
                 const uint32_t nc = ceil_div((uint64_t)fb->width * fb->height, kClearUnit);
@@ -243,11 +243,26 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         if (bp.vert_units + bp.face_units + bp.tile_units > 0) b->launches.push_back(L);
     }
     if (async) {
-        AXR_CUDA(ctx, cudaMemcpyAsync(d_table, table.data(), sizeof(BatchDraw) * table.size(), cudaMemcpyHostToDevice,
-                                      ctx->stream));
-        if (!units.empty())
-            AXR_CUDA(ctx, cudaMemcpyAsync(d_units, units.data(), sizeof(UnitRef) * units.size(), cudaMemcpyHostToDevice,
-                                          ctx->stream));
+        // through pinned staging, so that the copies are queued without waiting for the work
+        // already on the stream
+        const size_t tb = sizeof(BatchDraw) * table.size(), ub = sizeof(UnitRef) * units.size();
+        const int t = b->stage_next;
+        b->stage_next ^= 1;
+        if (!b->stage_done[t]) AXR_CUDA(ctx, cudaEventCreateWithFlags(&b->stage_done[t], cudaEventDisableTiming));
+        AXR_CUDA(ctx, cudaEventSynchronize(b->stage_done[t]));  // the upload two plans ago has been read
+        if (b->stage_bytes[t] < tb + ub) {
+            if (b->stage[t]) cudaFreeHost(b->stage[t]);
+            b->stage[t] = nullptr;
+            b->stage_bytes[t] = 0;
+            AXR_CUDA(ctx, cudaMallocHost(&b->stage[t], tb + ub));
+            b->stage_bytes[t] = tb + ub;
+        }
+        unsigned char* h = static_cast<unsigned char*>(b->stage[t]);
+        std::memcpy(h, table.data(), tb);
+        if (ub) std::memcpy(h + tb, units.data(), ub);
+        AXR_CUDA(ctx, cudaMemcpyAsync(d_table, h, tb, cudaMemcpyHostToDevice, ctx->stream));
+        if (ub) AXR_CUDA(ctx, cudaMemcpyAsync(d_units, h + tb, ub, cudaMemcpyHostToDevice, ctx->stream));
+        AXR_CUDA(ctx, cudaEventRecord(b->stage_done[t], ctx->stream));
     } else {
         AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         AXR_CUDA(ctx, cudaMemcpy(d_table, table.data(), sizeof(BatchDraw) * table.size(), cudaMemcpyHostToDevice));
@@ -271,15 +286,15 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
         bp.prof = ctx->profile && b->form == kFormPersistent ? ctx->batch_prof : nullptr;
         cudaEvent_t* ev = nullptr;
         if (ctx->profile && b->form == kFormPhased && !ctx->capturing) {
-            while (ctx->batch_events.size() < ctx->batch_events_used + 5) {
+            while (ctx->batch_events.size() < ctx->batch_events_used + 6) {
                 cudaEvent_t e;
                 AXR_CUDA(ctx, cudaEventCreate(&e));
                 ctx->batch_events.push_back(e);
             }
             ev = &ctx->batch_events[ctx->batch_events_used];
-            ctx->batch_events_used += 5;
+            ctx->batch_events_used += 6;
         }
-        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, ctx->stream, &ctx->aux, ev, &ctx->launches));
+        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, ctx->stream, ev, &ctx->launches));
     }
     return AXR_OK;
 }
@@ -345,6 +360,20 @@ void free_batch(axr_batch* b) {
     b->launches.clear();
 }
 
+void free_batch_staging(axr_batch* b) {
+    if (!b) return;
+    for (int t = 0; t < 2; ++t) {
+        if (b->stage_done[t]) {
+            cudaEventSynchronize(b->stage_done[t]);
+            cudaEventDestroy(b->stage_done[t]);
+        }
+        if (b->stage[t]) cudaFreeHost(b->stage[t]);
+        b->stage[t] = nullptr;
+        b->stage_done[t] = nullptr;
+        b->stage_bytes[t] = 0;
+    }
+}
+
 }  // namespace axr_internal
 
 extern "C" {
@@ -378,6 +407,7 @@ void axr_batch_destroy(axr_context* ctx, axr_batch* b) {
     DeviceGuard g(b->device);
     if (ctx && ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_batch(b);
+    free_batch_staging(b);
     delete b;
 }
 
@@ -486,6 +516,7 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
     }
     cudaStreamSynchronize(ctx->stream);
     free_batch(&trial);
+    free_batch_staging(&trial);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != AXR_OK) return st;

@@ -606,6 +606,7 @@ void axr_server_destroy(axr_server* srv) {
         for (auto& f : srv->fbs) srv->free_fb(*f);
         for (auto& s : srv->slots) {
             free_batch(&s->plan);
+            free_batch_staging(&s->plan);
             if (s->kernel_done) cudaEventDestroy(s->kernel_done);
             if (s->copies_done) cudaEventDestroy(s->copies_done);
         }

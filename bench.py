@@ -8,8 +8,8 @@ clearColor + clearDepth + drawMesh, through the C ABI.
                     [--workload batch|heightfield|sphere|soup] [--no-autotune]
 
 Default workload `batch`: a step renders the 512 draws of the mixed batch, each into its
-own framebuffer, with the batched form (one persistent launch, clears fused, replayed from
-a CUDA graph, raster parameter autotuned per density class); the plain per-draw path on
+own framebuffer, with the batched form (one set of launches over all draws, replayed from
+a CUDA graph; launch form and raster parameter autotuned); the plain per-draw path on
 the same draws is timed beside it (`plain`, `batched_vs_plain`). The single-draw workloads
 (`heightfield`, `sphere`, `soup`) time one frame per step through the per-draw path.
 
@@ -233,6 +233,15 @@ def pinned_like(lib, arr: np.ndarray, keep: list) -> np.ndarray:
     out = np.frombuffer(buf, dtype=arr.dtype).reshape(arr.shape)
     out[...] = arr
     return out
+
+
+def pinned_bytes(lib, nbytes: int, keep: list) -> np.ndarray:
+    """Uninitialised page-locked host bytes from the library's allocator."""
+    p = lib.axr_host_alloc(nbytes)
+    if not p:
+        raise MemoryError("axr_host_alloc failed")
+    keep.append(p)
+    return np.frombuffer((C.c_uint8 * nbytes).from_address(p), dtype=np.uint8)
 
 
 def cpu_baseline(scene, steps: int, budget_s: float):
@@ -477,13 +486,15 @@ def batch_algo_bytes(scenes, frags: float) -> float:
     return b
 
 
-def batch_phase_bytes(scenes, frags: float, tiles: int) -> dict:
+def batch_phase_bytes(scenes, frags: float, tiles: int, dirty: int, clear_apart: bool) -> dict:
     """Algorithmic bytes of each phase of one batched step (Blinn-Phong: 48-byte vertex
     cache entries): vertices read (32) + cache written (48) per vertex; indices (12 per
     face) + cache gathers (16 per vertex) + one key per covered fragment (8) for the face
-    and large phases together; the tile pass writes colour + depth once per pixel (8),
-    reads the flags (4 per tile), reads and resets the key of every covered pixel (16),
-    reads the vertex cache (48 per vertex) and min(texture, 4 per covered fragment)."""
+    and large phases together; the tile pass reads the flags (4 per tile), reads and resets
+    the key of every covered pixel (16), reads the vertex cache (48 per vertex) and
+    min(texture, 4 per covered fragment), and writes colour + depth (8 per pixel): of the
+    dirty tiles when the clear kernel has written every pixel before (its own 8 per pixel),
+    of every pixel otherwise."""
     total_faces = sum(int(sc.mesh.indices.shape[0]) for sc in scenes)
     v = f = px = tex = 0.0
     for sc in scenes:
@@ -493,8 +504,88 @@ def batch_phase_bytes(scenes, frags: float, tiles: int) -> dict:
         f += F
         px += sc.width * sc.height
         tex += min(t, 4.0 * frags * F / max(1, total_faces))
-    return {"vertex": 80.0 * v, "face": 12.0 * f + 16.0 * v + 8.0 * frags, "large": 8.0 * frags,
-            "tile": 8.0 * px + 4.0 * tiles + 16.0 * frags + 48.0 * v + tex}
+    written = 8.0 * 256 * dirty if clear_apart else 8.0 * px
+    return {"clear": 8.0 * px if clear_apart else 0.0, "vertex": 80.0 * v,
+            "face": 12.0 * f + 16.0 * v + 8.0 * frags, "large": 8.0 * frags,
+            "tile": written + 4.0 * tiles + 16.0 * frags + 48.0 * v + tex}
+
+
+def run_batch_png(ctx, lib, stream, flush, sets, tables, args, dist, keep) -> dict:
+    """End to end with PNG output, pipelined: two framebuffer sets; step k renders set k%2
+    (axr_draw_batch), enqueues its PNG encode (axr_png_batch_encode) and then copies the
+    files of step k-1 to pinned memory (axr_png_batch_read) while the GPU works on step k.
+    Timed over K steps plus the last read. Also the encode alone on the device (CUDA
+    events), against the HBM peak with its algorithmic bytes: each colour plane read once
+    (4 per pixel) and each file written."""
+    import torch
+
+    from axiomr_gb300 import api
+
+    draws = sets[0]
+    n = len(draws)
+    fb_lists = [(C.c_void_p * n)(*[d.framebuffer.handle.value for d in st]) for st in sets]
+    caps = [api.png_bound(d.framebuffer.width, d.framebuffer.height, 3) for d in draws]
+    host = [[pinned_bytes(lib, c, keep) for c in caps] for _ in sets]
+    ptrs = [(C.c_void_p * n)(*[h.ctypes.data for h in hs]) for hs in host]
+    capa = (C.c_uint64 * n)(*caps)
+    pngs = [api.PngBatch(ctx), api.PngBatch(ctx)]
+
+    def run(steps):
+        for k in range(steps):
+            cur = k % 2
+            api.draw_batch(ctx, tables[cur])
+            pngs[cur].encode(fb_lists[cur], 3)
+            if k:
+                pngs[1 - cur].read_into(ptrs[1 - cur], capa)
+        last = (steps - 1) % 2
+        pngs[last].read_into(ptrs[last], capa)
+
+    run(4)
+    torch.cuda.synchronize()
+    steps = max(3, args.steps // 2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    e0.record(stream)
+    run(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    total_ms = dist.max(float(e0.elapsed_time(e1)))
+    value = n * steps * dist.world / (total_ms / 1e3)
+    sizes = pngs[0].sizes()
+    file_bytes = int(sum(sizes))
+    pixels = sum(d.framebuffer.width * d.framebuffer.height for d in draws)
+    # the encode alone, into device buffers
+    bufs = [torch.empty((c + 255) // 256 * 256, dtype=torch.uint8, device=f"cuda:{dist.local_rank}") for c in caps]
+    dsz = torch.zeros(n, dtype=torch.int64, device=f"cuda:{dist.local_rank}")
+    outs = (C.c_void_p * n)(*[b.data_ptr() for b in bufs])
+    fb_arr = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in draws])
+    torch.cuda.synchronize()
+
+    def encode():
+        rc = lib.axr_framebuffers_encode_png(ctx.handle, n, fb_arr, 3, outs, capa, C.c_void_p(dsz.data_ptr()))
+        if rc != 0:
+            raise RuntimeError("axr_framebuffers_encode_png failed")
+
+    for _ in range(3):
+        encode()
+    enc_ms = timed_steps(stream, flush, max(3, args.steps // 2), encode)
+    enc = sum(enc_ms) / len(enc_ms)
+    hbm_peak, peak_kind = measured_peaks()
+    algo = 4.0 * pixels + file_bytes
+    del bufs
+    for pb in pngs:
+        pb.close()
+    return {"value": round(value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(n * C.sizeof(api.DrawDesc)),
+            "d2h_bytes_per_step": file_bytes + 8 * n,
+            "path": "per step: axr_draw_batch + axr_png_batch_encode of the 512 frames (RGB PNG files, encoded on "
+                    "the GPU, lossless), while the previous step's files are copied to pinned memory "
+                    "(axr_png_batch_read); two framebuffer sets, inputs larger than L2",
+            "steps": steps, "png_bytes_per_step": file_bytes, "rgb_bytes_per_step": 3 * pixels,
+            "encode_us": round(enc * 1e3, 2), "encode_launches": 4,
+            "encode_roofline": {"bound": "hbm", "achieved": round(algo / (enc * 1e-3) / 1e9, 1), "peak": hbm_peak,
+                                "peak_source": peak_kind, "unit": "GB/s",
+                                "frac": round(algo / (enc * 1e-3) / 1e9 / hbm_peak, 4), "algorithmic_bytes": algo,
+                                "definition": "4 bytes per pixel read + the file bytes written"}}
 
 
 def run_batch(args, dist: Dist):
@@ -581,31 +672,68 @@ def run_batch(args, dist: Dist):
     plain_value = n * len(plain_ms) / (sum(plain_ms) / 1e3)
     eager_value = n * len(eager_ms) / (sum(eager_ms) / 1e3)
 
-    # ---- end to end: per step the draw table goes up from the host (one-shot batch entry
-    # point) and every framebuffer (colour + depth) comes back to pinned host memory
-    # the step's result is the 512 rendered images: their colour planes come back (the depth
-    # planes stay on the device, as the reference's framebuffer keeps its depth)
+    # ---- end to end. The step's result is the 512 rendered images: per step the draw table
+    # goes up from the host (the one-shot batch entry point) and the colour planes come back
+    # to pinned host memory (the depth planes stay on the device, as the reference's
+    # framebuffer keeps its depth). Serial: draw, read back, next step. Pipelined: two
+    # framebuffer sets; step k renders set k%2 and starts its read-back on the read-back's
+    # own copy streams (axr_readback_start), then waits for step k-1's (axr_readback_wait),
+    # so the copies of one step overlap the rendering of the next.
     keep = []
-    outs = [pinned_like(lib, np.zeros((d.framebuffer.height, d.framebuffer.width, 4), np.uint8), keep) for d in draws]
-    d2h = sum(a.nbytes for a in outs)
+    sets = [draws, api.batch_draws(ctx, scenes, textures, meshes)]
+    tables = [api.draw_table(st) for st in sets]  # the host program's draw tables, uploaded every step
+    fb_arrs = [(C.c_void_p * n)(*[d.framebuffer.handle.value for d in st]) for st in sets]
+    outs = [[pinned_bytes(lib, d.framebuffer.width * d.framebuffer.height * 4, keep) for d in draws] for _ in sets]
+    bgra_arrs = [(C.c_void_p * n)(*[hb.ctypes.data for hb in o]) for o in outs]
+    d2h = sum(a.nbytes for a in outs[0])
     h2d = n * C.sizeof(api.DrawDesc)
-    fb_arr = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in draws])
-    bgra_arr = (C.c_void_p * n)(*[hb.ctypes.data for hb in outs])
+    fb_arr = fb_arrs[0]
 
     def e2e_step():
-        api.draw_batch(ctx, draws)
-        rc = lib.axr_framebuffers_read_async(ctx.handle, n, fb_arr, bgra_arr, None)
+        api.draw_batch(ctx, tables[0])
+        rc = lib.axr_framebuffers_read_async(ctx.handle, n, fb_arrs[0], bgra_arrs[0], None)
         if rc != 0:
             raise RuntimeError("axr_framebuffers_read_async failed")
 
     for _ in range(2):
         e2e_step()
     ctx.sync()
+    serial_ms = timed_steps(stream, flush, max(3, args.steps // 4), e2e_step)
+    serial_value = n * len(serial_ms) * dist.world / (dist.max(float(sum(serial_ms))) / 1e3)
+
+    rbs = []
+    for _ in sets:
+        h = C.c_void_p()
+        api.check(lib.axr_readback_create(ctx.handle, C.byref(h)), ctx.handle)
+        rbs.append(h)
+
+    def pipelined(steps):
+        for k in range(steps):
+            cur = k % 2
+            api.draw_batch(ctx, tables[cur])
+            api.check(lib.axr_readback_start(ctx.handle, rbs[cur], n, fb_arrs[cur], bgra_arrs[cur], None), ctx.handle)
+            if k:
+                api.check(lib.axr_readback_wait(ctx.handle, rbs[1 - cur]), ctx.handle)
+        api.check(lib.axr_readback_wait(ctx.handle, rbs[(steps - 1) % 2]), ctx.handle)
+
+    pipelined(4)
+    torch.cuda.synchronize()
+    e2e_steps = max(3, args.steps // 2)
     l0 = ctx.profile()["kernel_launches"]
-    e2e_ms = timed_steps(stream, flush, max(3, args.steps // 2), e2e_step)
-    ctx.sync()
-    e2e_launches = (ctx.profile()["kernel_launches"] - l0) / max(1, len(e2e_ms))
-    e2e_value = n * len(e2e_ms) * dist.world / (dist.max(float(sum(e2e_ms))) / 1e3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    e0.record(stream)
+    pipelined(e2e_steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_launches = (ctx.profile()["kernel_launches"] - l0) / e2e_steps
+    e2e_value = n * e2e_steps * dist.world / (dist.max(float(e0.elapsed_time(e1))) / 1e3)
+    for h in rbs:
+        lib.axr_readback_destroy(ctx.handle, h)
+
+    # ---- the same, with the frames delivered as PNG files encoded on the GPU (RGB, top row
+    # first: the picture the reference's window shows); only the files cross the link
+    png = run_batch_png(ctx, lib, stream, flush, sets, tables, args, dist, keep)
     for p in keep:
         lib.axr_host_free(p)
 
@@ -617,7 +745,7 @@ def run_batch(args, dist: Dist):
     pr = ctx.profile()
     ctx.profile(False)
     nl = max(1, pr["batch_launches"])
-    phase_ms = {k: pr[f"batch_{k}_ms"] / nl for k in ("vertex", "face", "large", "tile")}
+    phase_ms = {k: pr[f"batch_{k}_ms"] / nl for k in ("clear", "vertex", "face", "large", "tile")}
 
     fp32_tflops = ctx.fp32_peak_tflops()
     hbm_peak, peak_kind = measured_peaks()
@@ -631,10 +759,11 @@ def run_batch(args, dist: Dist):
     alu_tflops = alu_flop / (ms * 1e-3) / 1e12
     achieved = algo / (ms * 1e-3) / 1e9
     faces = info["faces"]
-    pb = batch_phase_bytes(scenes, frags, int(info["tiles"]))
+    pb = batch_phase_bytes(scenes, frags, int(info["tiles"]), int(st["tiles"]), info["form"] == 1)
     dom = max(phase_ms, key=phase_ms.get)
-    kernel_of = {"vertex": "batch_vertex_kernel", "face": "batch_face_kernel", "large": "batch_large_kernel",
-                 "tile": "batch_tile_kernel"} if info["form"] == 1 else {k: "batch_kernel" for k in phase_ms}
+    kernel_of = {"clear": "batch_clear_kernel", "vertex": "batch_vertex_kernel", "face": "batch_face_kernel",
+                 "large": "batch_large_kernel", "tile": "batch_tile_kernel"} if info["form"] == 1 else \
+        {k: "batch_kernel" for k in phase_ms}
     dom_achieved = pb[dom] / (phase_ms[dom] * 1e-3) / 1e9 if phase_ms[dom] > 0 else 0.0
     out = {
         "metric": "frames/s", "value": round(value, 2), "unit": "frames/s", "n_gpus": dist.world,
@@ -642,9 +771,10 @@ def run_batch(args, dist: Dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
         "config": {"workload": f"batch: {desc}",
-                   "form": ("batched, phased: four launches per step over the work units of all draws"
-                            if info["form"] == 1 else "batched, persistent: one cooperative launch per step")
-                   + " (clears fused into the tile pass), replayed from a CUDA graph",
+                   "form": ("batched, phased: a clear kernel and four phase launches per step over the work "
+                            "units of all draws" if info["form"] == 1 else
+                            "batched, persistent: one cooperative launch per step (clears fused into the tile pass)")
+                   + ", replayed from a CUDA graph",
                    "frames_per_step": n, "l2": "flushed before every timed step (256 MiB write, outside the events)",
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
                    "tuning_small_max_pixels": tuning},
@@ -661,10 +791,15 @@ def run_batch(args, dist: Dist):
         "batched_vs_plain": round(value / plain_value, 3),
         "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "path": "axr_draw_batch (draw table from the host) + read-back of all 512 rendered images "
-                        "(BGRA8 colour planes) into pinned memory (axr_framebuffers_read_async, 4 copy streams); "
-                        "meshes and textures resident",
-                "gpu_launches_per_step": e2e_launches},
+                "path": "per step axr_draw_batch (draw table from the host) + read-back of all 512 rendered "
+                        "images (BGRA8 colour planes) into pinned memory on 4 copy streams (axr_readback_start / "
+                        "axr_readback_wait), pipelined over two framebuffer sets so that step k's copies overlap "
+                        "step k+1's rendering; meshes and textures resident; inputs larger than L2",
+                "steps": e2e_steps, "gpu_launches_per_step": e2e_launches,
+                "serial": {"value": round(serial_value, 2), "unit": "frames/s",
+                           "path": "the same without overlap: draw, read back (axr_framebuffers_read_async), "
+                                   "next step; L2 flushed before each step"}},
+        "e2e_png": png,
         "gpu_launches": int(info["launches"]) * len(step_ms),
         "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),
                      "peak": hbm_peak, "peak_source": peak_kind, "unit": "GB/s",

@@ -193,11 +193,61 @@ axr_status axr_framebuffer_read_async(axr_context* ctx, const axr_framebuffer* f
  * waits for them. Use pinned memory and axr_sync. */
 axr_status axr_framebuffers_read_async(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
                                        uint8_t* const* bgra, float* const* depth);
+/* A read-back on its own copy streams (no reference counterpart), for pipelines:
+ * axr_readback_start enqueues the copies of axr_framebuffers_read_async after the work
+ * already on the context stream, but work enqueued later on the context stream does NOT
+ * wait for them, so the next frames render while these copy; do not draw into these
+ * framebuffers again before axr_readback_wait returns (it waits for the copies). */
+typedef struct axr_readback axr_readback;
+axr_status axr_readback_create(axr_context* ctx, axr_readback** out);
+void axr_readback_destroy(axr_context* ctx, axr_readback* rb);
+axr_status axr_readback_start(axr_context* ctx, axr_readback* rb, int32_t count, const axr_framebuffer* const* fbs,
+                              uint8_t* const* bgra, float* const* depth);
+axr_status axr_readback_wait(axr_context* ctx, axr_readback* rb);
 /* Upload host colour and/or depth into the framebuffer (either may be NULL). */
 axr_status axr_framebuffer_write(axr_context* ctx, axr_framebuffer* fb, const uint8_t* bgra, const float* depth);
 axr_status axr_framebuffer_size(const axr_framebuffer* fb, int32_t* width, int32_t* height);
 /* Device pointers of the colour (uint32 per pixel) and depth planes, for interop. */
 axr_status axr_framebuffer_device_pointers(const axr_framebuffer* fb, void** bgra, void** depth);
+
+/* ------------------------------------------------------------------ output encoding
+ * Headless counterpart of Window::present (src/window.cpp:70-84), which copies the BGRA8
+ * colour plane into a bottom-up 32-bit DIB (src/windows_bitmap.cpp:15-30) and shows it:
+ * each framebuffer's colour plane becomes a PNG file, top row first (framebuffer row
+ * height-1 is the file's first scanline), channels 3 = RGB8 (the picture the window
+ * shows, alpha dropped) or 4 = RGBA8. Lossless; one deflate stream with the fixed Huffman
+ * codes and run/row matches, so flat regions compress and detailed ones stay near 3 or 4
+ * bytes per pixel.
+ *
+ * Worst-case file size of a width x height image (0 for bad arguments). */
+uint64_t axr_png_bound(uint32_t width, uint32_t height, uint32_t channels);
+/* Encode `count` framebuffers into device buffers out[i] (16-byte aligned, capacity[i] >=
+ * axr_png_bound) on the context stream, after the work already enqueued there; sizes is
+ * a device array of `count` file sizes, written by the encode. Four kernel launches for
+ * the whole list. */
+axr_status axr_framebuffers_encode_png(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
+                                       uint32_t channels, void* const* out, const uint64_t* capacity,
+                                       uint64_t* sizes);
+/* Encode into internal device buffers and copy the files to host memory: sizes[i] (host)
+ * receives file i's size and files[i] (capacity[i] bytes; pinned memory copies fastest)
+ * the file. With files NULL only the sizes are returned. AXR_E_INVALID, with the sizes
+ * filled in, when a host buffer is too small. Returns when the files are on the host. */
+axr_status axr_framebuffers_read_png(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
+                                     uint32_t channels, void* const* files, const uint64_t* capacity,
+                                     uint64_t* sizes);
+/* The same read-back in steps, for pipelines: a batch keeps its files on the device and has
+ * its own copy streams. axr_png_batch_encode enqueues the encode of `count` framebuffers on
+ * the context stream (after the work already there, and after this batch's previous files
+ * were read) and returns at once; axr_png_batch_sizes waits for that encode and returns the
+ * file sizes; axr_png_batch_read copies the files to host buffers (capacity[i] bytes each)
+ * and returns when they are there. Render and encode batch k+1 while reading batch k. */
+typedef struct axr_png_batch axr_png_batch;
+axr_status axr_png_batch_create(axr_context* ctx, axr_png_batch** out);
+void axr_png_batch_destroy(axr_context* ctx, axr_png_batch* batch);
+axr_status axr_png_batch_encode(axr_context* ctx, axr_png_batch* batch, int32_t count,
+                                const axr_framebuffer* const* fbs, uint32_t channels);
+axr_status axr_png_batch_sizes(axr_context* ctx, axr_png_batch* batch, uint64_t* sizes);
+axr_status axr_png_batch_read(axr_context* ctx, axr_png_batch* batch, void* const* files, const uint64_t* capacity);
 
 /* ------------------------------------------------------------------ pipeline state
  * Pipeline::setShader / setCamera / setFramebuffer (include/pipeline.hpp:22-24). The
@@ -430,6 +480,48 @@ axr_status axr_camera_matrices(const float position[3], const float target[3], f
                                float view[16], float projection[16], float view_proj[16]);
 axr_status axr_viewport_matrix(int32_t x, int32_t y, int32_t width, int32_t height, float out[16]);
 
+/* The reference Camera as caller-owned state (include/camera.hpp:6-67, src/camera.cpp:
+ * 30-205): construction, setters, mouse / keyboard input and update(deltaTime), with the
+ * reference's float operation order and behaviour, including: the view matrix stays
+ * identity until the first update; setFov / setAspectRatio mark the projection dirty but
+ * nothing recomputes it, so they do not change the matrices; update rotates only when both
+ * mouse deltas are non-zero; movement is the sum of unit direction vectors per second. */
+typedef struct axr_camera_state {
+    float position[3];
+    float orientation[4];      /* quaternion x, y, z, w */
+    float forward[3], right[3], up[3];
+    float delta_yaw, delta_pitch;  /* degrees per second from the last input */
+    float velocity[3];
+    float fov_degrees, aspect_ratio, near_plane, far_plane;
+    float movement_speed, mouse_sensitivity;
+    float last_mouse[2];
+    int32_t viewport[4];       /* x, y, width, height */
+    float view[16], projection[16], view_proj[16];
+    int32_t view_dirty, projection_dirty;
+} axr_camera_state;
+
+/* What Camera::handleInput reads from the Window (include/window.hpp:20-22). */
+typedef struct axr_input_state {
+    float mouse[2];
+    uint8_t mouse_buttons[3];  /* left, right, middle */
+    uint8_t keys[256];         /* indexed by the key's character, as Window::isKeyDown */
+} axr_input_state;
+
+/* Camera(position, target, fov, aspect) */
+axr_status axr_camera_init(axr_camera_state* cam, const float position[3], const float target[3], float fov_degrees,
+                           float aspect_ratio);
+axr_status axr_camera_set_position(axr_camera_state* cam, const float position[3]);
+axr_status axr_camera_set_target(axr_camera_state* cam, const float target[3]);
+axr_status axr_camera_set_fov(axr_camera_state* cam, float fov_degrees);
+axr_status axr_camera_set_aspect_ratio(axr_camera_state* cam, float aspect_ratio);
+axr_status axr_camera_set_viewport(axr_camera_state* cam, int32_t x, int32_t y, int32_t width, int32_t height);
+/* Camera::handleInput(window) */
+axr_status axr_camera_handle_input(axr_camera_state* cam, const axr_input_state* input);
+/* Camera::update(deltaTime) */
+axr_status axr_camera_update(axr_camera_state* cam, float delta_time);
+/* What drawMesh reads from the camera: view-projection, viewport matrix, position. */
+axr_status axr_camera_describe(const axr_camera_state* cam, axr_camera_desc* out);
+
 /* ------------------------------------------------------------------ statistics
  * Counters of the draws issued since the last reset (collection slows the kernels a
  * little and is off by default). */
@@ -463,7 +555,8 @@ typedef struct axr_profile {
     double batch_vertex_ms;  /* batched kernel phases: vertices */
     double batch_face_ms;    /*   faces (clip, cull, setup, small-triangle raster) */
     double batch_large_ms;   /*   large-triangle tiles */
-    double batch_tile_ms;    /*   tile pass (key scan, shading, fused clears, write-out) */
+    double batch_tile_ms;    /*   tile pass (key scan, shading, write-out; clears of the persistent form) */
+    double batch_clear_ms;   /*   clear kernel of the phased form (fully cleared draws) */
 } axr_profile;
 axr_status axr_profile_enable(axr_context* ctx, int32_t enable);
 axr_status axr_profile_read(axr_context* ctx, axr_profile* out);

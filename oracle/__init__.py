@@ -176,6 +176,24 @@ class Oracle:
         self.lib.ref_obj_fetch(verts.ctypes.data, faces.ctypes.data, groups.ctypes.data)
         return verts[: counts[0]], faces[: counts[1]], groups[: counts[2]]
 
+    def camera_script(self, cam, ops) -> np.ndarray:
+        """Reference only: the Camera driven by a script of operations (rows of 6 floats:
+        kind, a0..a3, flags; kinds 0 update(dt), 1 handleInput(mouse x, y; flags bit 0 right
+        button, bits 1-4 keys W S A D), 2 setPosition, 3 setTarget, 4 setFov,
+        5 setAspectRatio, 6 setViewport) -> (n, 51): view, projection, viewProjection and
+        position after each operation."""
+        if self.kind != "ref":
+            raise ValueError("camera_script runs the reference Camera")
+        ops = np.ascontiguousarray(ops, np.float32).reshape(-1, 6)
+        out = np.zeros((ops.shape[0], 51), np.float32)
+        c = make_camera(cam)
+        f = self.lib.ref_camera_script
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        f.restype = C.c_int
+        if f(C.addressof(c), ops.ctypes.data, ops.shape[0], out.ctypes.data) != 0:
+            raise RuntimeError("bad camera script")
+        return out
+
     # -- stages -----------------------------------------------------------------------
     def camera(self, cam) -> np.ndarray:
         """(3, 16) float32: view, projection, viewProjection (column-major)."""

@@ -25,12 +25,6 @@
 
 #include "axo.h"
 
-// camera.cpp's handleInput (reference src/camera.cpp:102-130) references two
-// out-of-line Window methods defined in window.cpp (Win32, not compiled). The oracle
-// never calls handleInput; these definitions only satisfy the linker.
-bool AR::Window::isMouseButtonDown(int) const { return false; }
-bool AR::Window::isKeyDown(char) const { return false; }
-
 namespace {
 
 // Standard-conforming access to private data members: explicit template instantiation
@@ -52,6 +46,9 @@ struct TexHeight { using type = int AR::Texture::*; friend type member(TexHeight
 struct TexChannels { using type = int AR::Texture::*; friend type member(TexChannels); };
 struct CamViewProj { using type = glm::mat4 AR::Camera::*; friend type member(CamViewProj); };
 struct CamPosition { using type = glm::vec3 AR::Camera::*; friend type member(CamPosition); };
+struct WinMouse { using type = glm::vec2 AR::Window::*; friend type member(WinMouse); };
+struct WinButtons { using type = bool (AR::Window::*)[3]; friend type member(WinButtons); };
+struct WinKeys { using type = bool (AR::Window::*)[256]; friend type member(WinKeys); };
 template struct Expose<MeshVertices, &AR::Mesh::m_Vertices>;
 template struct Expose<MeshFaces, &AR::Mesh::m_Faces>;
 template struct Expose<MeshMaterials, &AR::Mesh::m_Materials>;
@@ -62,6 +59,9 @@ template struct Expose<TexHeight, &AR::Texture::m_Height>;
 template struct Expose<TexChannels, &AR::Texture::m_Channels>;
 template struct Expose<CamViewProj, &AR::Camera::m_ViewProjection>;
 template struct Expose<CamPosition, &AR::Camera::m_Position>;
+template struct Expose<WinMouse, &AR::Window::m_MousePos>;
+template struct Expose<WinButtons, &AR::Window::m_MouseButtons>;
+template struct Expose<WinKeys, &AR::Window::m_Keys>;
 
 // Pipeline::clipTriangle is protected static (reference include/pipeline.hpp:34-42).
 struct ClipAccess : AR::Pipeline {
@@ -309,7 +309,71 @@ int draw_with_camera(AR::Camera& cam, const axo_mesh* mesh, const float* model, 
 
 }  // namespace
 
+// camera.cpp's handleInput (reference src/camera.cpp:102-130) calls two out-of-line Window
+// methods defined in window.cpp (Win32, not compiled here); these read the same members
+// the Win32 message handler fills in.
+bool AR::Window::isMouseButtonDown(int button) const { return (this->*member(WinButtons()))[button]; }
+bool AR::Window::isKeyDown(char key) const { return (this->*member(WinKeys()))[static_cast<unsigned char>(key)]; }
+
+namespace {
+
+// A Window whose input members are set directly: storage for the object without running
+// its Win32 constructor (only the input members are ever read).
+struct FakeWindow {
+    alignas(AR::Window) unsigned char bytes[sizeof(AR::Window)] = {};
+    AR::Window& get() { return *reinterpret_cast<AR::Window*>(bytes); }
+    void set(float mx, float my, int flags) {
+        AR::Window& w = get();
+        w.*member(WinMouse()) = glm::vec2(mx, my);
+        bool(&b)[3] = w.*member(WinButtons());
+        bool(&k)[256] = w.*member(WinKeys());
+        for (bool& x : b) x = false;
+        for (bool& x : k) x = false;
+        b[1] = (flags & 1) != 0;
+        k[(unsigned char)'W'] = (flags & 2) != 0;
+        k[(unsigned char)'S'] = (flags & 4) != 0;
+        k[(unsigned char)'A'] = (flags & 8) != 0;
+        k[(unsigned char)'D'] = (flags & 16) != 0;
+    }
+};
+
+}  // namespace
+
 extern "C" {
+
+// A camera script: Camera(position, target, fov, aspect) + setViewport, then per op
+// (6 floats: kind, a0..a3, flags) one of update(a0), handleInput(mouse a0 a1; flags bit 0
+// right button, bits 1-4 keys W S A D), setPosition, setTarget, setFov, setAspectRatio,
+// setViewport; after each op the view, projection, viewProjection (16 floats each) and the
+// position (3): 51 floats per op.
+int ref_camera_script(const axo_camera* c, const float* ops, int n, float* out) {
+    AR::Camera cam(glm::vec3(c->position[0], c->position[1], c->position[2]),
+                   glm::vec3(c->target[0], c->target[1], c->target[2]), c->fov_degrees, c->aspect);
+    cam.setViewport(c->viewport[0], c->viewport[1], c->viewport[2], c->viewport[3]);
+    FakeWindow win;
+    for (int i = 0; i < n; ++i) {
+        const float* o = ops + 6 * i;
+        switch ((int)o[0]) {
+            case 0: cam.update(o[1]); break;
+            case 1: win.set(o[1], o[2], (int)o[5]); cam.handleInput(win.get()); break;
+            case 2: cam.setPosition(glm::vec3(o[1], o[2], o[3])); break;
+            case 3: cam.setTarget(glm::vec3(o[1], o[2], o[3])); break;
+            case 4: cam.setFov(o[1]); break;
+            case 5: cam.setAspectRatio(o[1]); break;
+            case 6: cam.setViewport((int)o[1], (int)o[2], (int)o[3], (int)o[4]); break;
+            default: return -1;
+        }
+        float* r = out + 51 * i;
+        store_mat4(cam.getViewMatrix(), r);
+        store_mat4(cam.getProjectionMatrix(), r + 16);
+        store_mat4(cam.getViewProjectionMatrix(), r + 32);
+        const glm::vec3 p = cam.getPosition();
+        r[48] = p.x;
+        r[49] = p.y;
+        r[50] = p.z;
+    }
+    return 0;
+}
 
 // view, projection, viewProjection (column-major, 16 floats each) of a reference Camera.
 int ref_camera(const axo_camera* c, float* out48) {

@@ -8,6 +8,7 @@ tests on another machine feed exactly the same bytes to the code under test.
 
     python tests/golden/make_golden.py        # rewrites tests/golden/*.npz
     python tests/golden/make_golden.py obj    # rewrites only the mesh-ingest fixtures
+    python tests/golden/make_golden.py camera # rewrites only the camera-script fixture
 """
 from __future__ import annotations
 
@@ -102,14 +103,33 @@ def make_obj_goldens(ref):
             print(f"obj_{name:12s} vertices={verts.shape[0]} faces={faces.shape[0]} groups={groups.tolist()}")
 
 
+def make_camera_goldens(ref):
+    """The reference Camera driven by seeded scripts (tests/camscript.py): matrices and
+    position after every operation."""
+    sys.path.insert(0, str(HERE.parent))
+    import camscript
+
+    arrays = {}
+    for k, (pos, tgt, fov, aspect) in enumerate(camscript.STARTS):
+        ops = camscript.script(7000 + k, n=120)
+        arrays[f"ops_{k}"] = ops
+        arrays[f"out_{k}"] = ref.camera_script(W.Camera(pos, tgt, fov, aspect, (0, 0, 800, 600)), ops)
+    np.savez_compressed(HERE / "camera_scripts.npz", **arrays)
+    print("camera scripts:", len(camscript.STARTS))
+
+
 def main():
     ref = Oracle("ref")
     if sys.argv[1:] == ["obj"]:
         make_obj_goldens(ref)
         return
+    if sys.argv[1:] == ["camera"]:
+        make_camera_goldens(ref)
+        return
     for old in HERE.glob("*.npz"):
         old.unlink()
     make_obj_goldens(ref)
+    make_camera_goldens(ref)
     for i, sc in enumerate(scene_list()):
         vp = ref.camera(sc.camera)[2]
         if sc.name == "sphere_close":

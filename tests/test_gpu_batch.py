@@ -223,3 +223,38 @@ def test_framebuffers_read_async_matches_single_reads(ctx):
             assert np.array_equal(outs[k][1].view(np.uint32), single[k][1].view(np.uint32))
         else:
             assert not outs[k][1].any()  # depth not requested
+
+
+def test_detached_readback_pipeline(ctx):
+    """axr_readback_start / wait: copies on the read-back's own streams while the next batch
+    renders into another framebuffer set; each set comes back as its own frames."""
+    import ctypes as C
+
+    scenes = small_batch(count=5, seed=23)
+    sets = [api.batch_draws(ctx, scenes), api.batch_draws(ctx, scenes[::-1])]
+    n = len(scenes)
+    expect = []
+    for st in sets:
+        api.draw_batch(ctx, st)
+        expect.append([d.framebuffer.read()[0] for d in st])
+    for st in sets:  # clear them again
+        for d in st:
+            d.framebuffer.clearColor(0, 0, 0, 0)
+    ctx.sync()
+    rbs = []
+    for _ in sets:
+        h = C.c_void_p()
+        api.check(ctx.lib.axr_readback_create(ctx.handle, C.byref(h)), ctx.handle)
+        rbs.append(h)
+    outs = [[np.zeros((d.framebuffer.height, d.framebuffer.width, 4), np.uint8) for d in st] for st in sets]
+    for k, st in enumerate(sets):
+        api.draw_batch(ctx, st)
+        fbs = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in st])
+        bgra = (C.c_void_p * n)(*[o.ctypes.data for o in outs[k]])
+        api.check(ctx.lib.axr_readback_start(ctx.handle, rbs[k], n, fbs, bgra, None), ctx.handle)
+    for k in range(2):
+        api.check(ctx.lib.axr_readback_wait(ctx.handle, rbs[k]), ctx.handle)
+        for got, want in zip(outs[k], expect[k]):
+            assert np.array_equal(got, want)
+    for h in rbs:
+        ctx.lib.axr_readback_destroy(ctx.handle, h)
