@@ -123,12 +123,14 @@ class ServerRequest(C.Structure):
     _fields_ = [("mesh", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("model", C.c_float * 16),
                 ("camera", CameraDesc), ("shader", ShaderDesc), ("clear_flags", C.c_uint32),
                 ("clear_rgba", C.c_uint8 * 4), ("clear_depth", C.c_float), ("arrival_ns", C.c_uint64),
-                ("out_bgra", C.c_void_p), ("out_depth", C.c_void_p)]
+                ("out_bgra", C.c_void_p), ("out_depth", C.c_void_p), ("png_channels", C.c_uint32),
+                ("out_png", C.c_void_p), ("out_png_capacity", C.c_uint64)]
 
 
 class ServerResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("batch_size", C.c_uint32), ("arrival_ns", C.c_uint64),
-                ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64), ("batch_id", C.c_uint64)]
+                ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64), ("batch_id", C.c_uint64),
+                ("png_bytes", C.c_uint64)]
 
 
 class ServerStats(C.Structure):

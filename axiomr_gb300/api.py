@@ -708,7 +708,8 @@ class Server:
 
     def submit(self, mesh_id: int, camera: "Camera", shader: Shader, width: int, height: int, model=None,
                clear_color=(0, 0, 0, 255), clear_depth: float = float("inf"), out_bgra: Optional[np.ndarray] = None,
-               out_depth: Optional[np.ndarray] = None, arrival_ns: int = 0) -> int:
+               out_depth: Optional[np.ndarray] = None, arrival_ns: int = 0, png_channels: int = 0,
+               out_png: Optional[np.ndarray] = None) -> int:
         r = _lib.ServerRequest()
         r.mesh = int(mesh_id)
         r.width, r.height = int(width), int(height)
@@ -726,6 +727,9 @@ class Server:
         r.arrival_ns = int(arrival_ns)
         r.out_bgra = _ptr(out_bgra)
         r.out_depth = _ptr(out_depth)
+        r.png_channels = int(png_channels)
+        r.out_png = _ptr(out_png)
+        r.out_png_capacity = 0 if out_png is None else int(out_png.nbytes)
         t = C.c_uint64()
         self._check(self.lib.axr_server_submit(self.handle, C.byref(r), C.byref(t)))
         return t.value

@@ -28,6 +28,15 @@ axr_status batch_plan(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
 axr_status batch_launch(axr_context* ctx, const axr_batch* b);
 // Release the PNG encoder's scratch (the caller synchronises first).
 void free_png(axr_context* ctx);
+// PNG batches for the serving loop, without blocking: create / release; enqueue an encode
+// (the caller holds ctx->mu); query whether the encode and its size copy are done
+// (cudaErrorNotReady while not); then file i's device address and size (0: overflow).
+axr_status png_batch_create(axr_context* ctx, axr_png_batch** out);
+void png_batch_release(axr_png_batch* b);
+axr_status png_batch_encode_locked(axr_context* ctx, axr_png_batch* b, int32_t count,
+                                   const axr_framebuffer* const* fbs, uint32_t channels);
+cudaError_t png_batch_query(const axr_png_batch* b);
+void png_batch_file(const axr_png_batch* b, int32_t i, const void** dev, uint64_t* size);
 
 template <class T>
 cudaError_t dmalloc(T** p, size_t count) {

@@ -1123,6 +1123,30 @@ axr_status batch_read(axr_context* ctx, axr_png_batch* b, void* const* files, co
 
 }  // namespace
 
+namespace axr_internal {
+
+axr_status png_batch_create(axr_context* ctx, axr_png_batch** out) { return create_batch(ctx, out); }
+
+void png_batch_release(axr_png_batch* b) {
+    if (b) release_batch(b);
+}
+
+axr_status png_batch_encode_locked(axr_context* ctx, axr_png_batch* b, int32_t count,
+                                   const axr_framebuffer* const* fbs, uint32_t channels) {
+    return batch_encode_locked(ctx, b, count, fbs, channels);
+}
+
+cudaError_t png_batch_query(const axr_png_batch* b) {
+    return b->encoded ? cudaEventQuery(b->done) : cudaSuccess;
+}
+
+void png_batch_file(const axr_png_batch* b, int32_t i, const void** dev, uint64_t* size) {
+    *dev = b->files + b->at[(size_t)i];
+    *size = b->sizes_host[i];
+}
+
+}  // namespace axr_internal
+
 extern "C" axr_status axr_png_batch_create(axr_context* ctx, axr_png_batch** out) {
     if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(ctx->mu);

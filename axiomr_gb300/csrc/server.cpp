@@ -104,6 +104,8 @@ struct Req {
     uint64_t arrival = 0, launch = 0, done = 0, batch_id = 0;
     uint32_t batch_size = 0;
     int status = AXR_OK;
+    int png_status = AXR_OK;  // the PNG file did not fit its buffer, or the encode failed
+    uint64_t png_bytes = 0;
     bool finished = false;
     Fb* fb = nullptr;
 };
@@ -112,6 +114,13 @@ struct Slot {
     axr_batch plan;
     std::vector<Req*> reqs;
     cudaEvent_t kernel_done = nullptr, copies_done = nullptr;
+    // PNG outputs: the RGB and RGBA files of the slot's requests, encoded right after the
+    // batch on the context stream; their copies are issued on the copy stream once the
+    // encode is done (its sizes are then known), behind the raw read-backs
+    axr_png_batch* png[2] = {};
+    std::vector<Req*> png_reqs[2];
+    cudaEvent_t files_done = nullptr;
+    bool files_pending = false, files_issued = false;
     bool busy = false;
     uint64_t id = 0;
 };
@@ -437,6 +446,24 @@ struct axr_server {
             if (st != AXR_OK) return st;
             if ((st = batch_launch(ctx, &s.plan)) != AXR_OK) return st;
         }
+        // PNG files of the requests that ask for them, encoded behind the kernels
+        s.files_pending = false;
+        s.files_issued = false;
+        for (int c = 0; c < 2; ++c) {
+            s.png_reqs[c].clear();
+            for (Req* q : s.reqs)
+                if (q->r.png_channels == (uint32_t)(3 + c)) s.png_reqs[c].push_back(q);
+            if (s.png_reqs[c].empty()) continue;
+            axr_status st = s.png[c] ? AXR_OK : png_batch_create(ctx, &s.png[c]);
+            std::vector<const axr_framebuffer*> f;
+            for (Req* q : s.png_reqs[c]) f.push_back(&q->fb->fb);
+            if (st == AXR_OK) {
+                std::lock_guard<std::mutex> lk(ctx->mu);
+                st = png_batch_encode_locked(ctx, s.png[c], (int32_t)f.size(), f.data(), (uint32_t)(3 + c));
+            }
+            if (st != AXR_OK) return st;
+            s.files_pending = true;
+        }
         // read-backs on the copy stream, behind the kernels
         e = cudaEventRecord(s.kernel_done, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(copy, s.kernel_done, 0);
@@ -457,11 +484,42 @@ struct axr_server {
     }
 
     void finish(Req& q, int status) {
-        q.status = status;
+        q.status = status != AXR_OK ? status : q.png_status;
         q.done = steady_ns();
         q.finished = true;
         release(q);
         ++stats.completed;
+    }
+
+    // Issue the copies of a slot's PNG files once their encode is done; false while not.
+    bool issue_files(Slot& s) {
+        for (int c = 0; c < 2; ++c)
+            if (!s.png_reqs[c].empty() && png_batch_query(s.png[c]) == cudaErrorNotReady) return false;
+        cudaError_t e = cudaSuccess;
+        for (int c = 0; c < 2; ++c) {
+            for (size_t i = 0; i < s.png_reqs[c].size(); ++i) {
+                Req* q = s.png_reqs[c][i];
+                const void* dev = nullptr;
+                uint64_t size = 0;
+                png_batch_file(s.png[c], (int32_t)i, &dev, &size);
+                q->png_bytes = size;
+                if (size == 0) {
+                    q->png_status = AXR_E_CUDA;
+                } else if (size > q->r.out_png_capacity) {
+                    q->png_status = AXR_E_CAPACITY;
+                } else if (e == cudaSuccess) {
+                    e = cudaMemcpyAsync(q->r.out_png, dev, size, cudaMemcpyDeviceToHost, copy);
+                }
+            }
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(s.files_done, copy);
+        if (e != cudaSuccess) {
+            error = std::string("PNG read-back: ") + cudaGetErrorString(e);
+            for (int c = 0; c < 2; ++c)
+                for (Req* q : s.png_reqs[c]) q->png_status = AXR_E_CUDA;
+        }
+        s.files_issued = true;
+        return true;
     }
 
     // Retire the busy slots whose read-backs are done (in launch order).
@@ -470,7 +528,8 @@ struct axr_server {
         for (auto& sp : slots) {
             Slot& s = *sp;
             if (!s.busy) continue;
-            const cudaError_t e = cudaEventQuery(s.copies_done);
+            if (s.files_pending && !s.files_issued && !issue_files(s)) continue;
+            cudaError_t e = cudaEventQuery(s.files_pending ? s.files_done : s.copies_done);
             if (e == cudaErrorNotReady) continue;
             const int status = e == cudaSuccess ? AXR_OK : AXR_E_CUDA;
             if (e != cudaSuccess) error = std::string("batch: ") + cudaGetErrorString(e);
@@ -571,6 +630,7 @@ axr_status axr_server_create(const axr_server_config* cfg, axr_server** out) {
         auto s = std::make_unique<Slot>();
         e = cudaEventCreateWithFlags(&s->kernel_done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->copies_done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->files_done, cudaEventDisableTiming);
         srv->slots.push_back(std::move(s));
     }
     if (e != cudaSuccess) {
@@ -609,6 +669,8 @@ void axr_server_destroy(axr_server* srv) {
             free_batch_staging(&s->plan);
             if (s->kernel_done) cudaEventDestroy(s->kernel_done);
             if (s->copies_done) cudaEventDestroy(s->copies_done);
+            if (s->files_done) cudaEventDestroy(s->files_done);
+            for (axr_png_batch* b : s->png) png_batch_release(b);
         }
         cudaStreamSynchronize(srv->ctx->stream);
         if (srv->uploaded) cudaEventDestroy(srv->uploaded);
@@ -686,6 +748,9 @@ axr_status axr_server_submit(axr_server* srv, const axr_server_request* r, uint6
         return fail(nullptr, AXR_E_INVALID, "request %dx%d", r->width, r->height);
     if (r->shader.kind < AXR_SHADER_FLAT || r->shader.kind > AXR_SHADER_GOURAUD)
         return fail(nullptr, AXR_E_INVALID, "unknown shader kind %d", r->shader.kind);
+    if (r->png_channels != 0 && r->png_channels != 3 && r->png_channels != 4)
+        return fail(nullptr, AXR_E_INVALID, "png_channels must be 0, 3 or 4");
+    if (r->png_channels && !r->out_png) return fail(nullptr, AXR_E_INVALID, "a PNG request needs out_png");
     auto q = std::make_unique<Req>();
     q->r = *r;
     q->arrival = r->arrival_ns ? r->arrival_ns : steady_ns();
@@ -719,6 +784,7 @@ axr_status axr_server_wait(axr_server* srv, uint64_t ticket, int32_t timeout_ms,
     out->launch_ns = q->launch;
     out->done_ns = q->done;
     out->batch_id = q->batch_id;
+    out->png_bytes = q->png_bytes;
     srv->reqs.erase(it);
     return AXR_OK;
 }

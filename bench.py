@@ -79,7 +79,7 @@ def parse_args():
     ap.add_argument("--rates", default="100,500,2000,5000", help="serve: offered loads, requests/s")
     ap.add_argument("--serve-seconds", type=float, default=30.0, help="serve: duration of each offered load")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: device-memory residency budget")
-    ap.add_argument("--readback", choices=("colour", "none"), default="colour",
+    ap.add_argument("--readback", choices=("colour", "png", "none"), default="colour",
                     help="serve: read each request's colour plane back to host memory, or not")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -850,13 +850,20 @@ def run_serve(args, dist: Dist):
         keep = []
         lib = srv.lib
         if args.readback == "colour":
-            ring = [pinned_like(lib, np.zeros((2160, 3840, 4), np.uint8), keep) for _ in range(96)]
-            hf_ring = [pinned_like(lib, np.zeros((1080, 1920, 4), np.uint8), keep) for _ in range(16)]
+            ring = [pinned_bytes(lib, 3840 * 2160 * 4, keep).reshape(2160, 3840, 4) for _ in range(96)]
+            hf_ring = [pinned_bytes(lib, 1920 * 1080 * 4, keep).reshape(1080, 1920, 4) for _ in range(16)]
+        elif args.readback == "png":  # RGB PNG files encoded on the GPU instead of the raw plane
+            ring = [pinned_bytes(lib, api.png_bound(3840, 2160, 3), keep) for _ in range(96)]
+            hf_ring = [pinned_bytes(lib, api.png_bound(1920, 1080, 3), keep) for _ in range(16)]
         else:
             ring, hf_ring = [None], [None]
+
+        def out(buf):
+            return {"png_channels": 3, "out_png": buf} if args.readback == "png" else {"out_bgra": buf}
+
         # warm-up: every asset resident once, framebuffer pools filled
-        ts = [srv.submit(i, cam_soup, gouraud, 3840, 2160, out_bgra=ring[k % len(ring)]) for k, i in enumerate(soup_ids)]
-        ts.append(srv.submit(hf_id, api.Camera.from_workload(hf.camera), blinn, 1920, 1080, out_bgra=hf_ring[0]))
+        ts = [srv.submit(i, cam_soup, gouraud, 3840, 2160, **out(ring[k % len(ring)])) for k, i in enumerate(soup_ids)]
+        ts.append(srv.submit(hf_id, api.Camera.from_workload(hf.camera), blinn, 1920, 1080, **out(hf_ring[0])))
         for t in ts:
             srv.wait(t)
         per_rate = []
@@ -876,12 +883,12 @@ def run_serve(args, dist: Dist):
                 while k < n and t0 + int(offs[k]) <= now:
                     if kinds[k]:
                         tickets[k] = srv.submit(soup_ids[which[k]], cam_soup, gouraud, 3840, 2160,
-                                                out_bgra=ring[soup_slot % len(ring)], arrival_ns=t0 + int(offs[k]))
+                                                arrival_ns=t0 + int(offs[k]), **out(ring[soup_slot % len(ring)]))
                         soup_slot += 1
                     else:
                         c = W.orbit_camera(2.5, 30.0, float(az[k]), 1920, 1080)
                         tickets[k] = srv.submit(hf_id, api.Camera.from_workload(c), blinn, 1920, 1080,
-                                                out_bgra=hf_ring[hf_slot % len(hf_ring)], arrival_ns=t0 + int(offs[k]))
+                                                arrival_ns=t0 + int(offs[k]), **out(hf_ring[hf_slot % len(hf_ring)]))
                         hf_slot += 1
                     k += 1
                 if k < n:

@@ -427,6 +427,11 @@ typedef struct axr_server_request {
     uint64_t arrival_ns;      /* arrival time on the server clock (0: the submit time) */
     uint8_t* out_bgra;        /* host destination of the colour plane (W*H*4), or NULL */
     float* out_depth;         /* host destination of the depth plane (W*H), or NULL */
+    uint32_t png_channels;    /* 3 / 4: also (or instead) return the colour plane as an RGB /
+                                 RGBA PNG file (axr_framebuffers_read_png), encoded right after
+                                 its batch and copied while the next batch renders; 0: none */
+    uint8_t* out_png;         /* host destination of the file */
+    uint64_t out_png_capacity;/* its bytes; axr_png_bound(W, H, channels) always suffices */
 } axr_server_request;
 
 typedef struct axr_server_result {
@@ -436,6 +441,7 @@ typedef struct axr_server_result {
     uint64_t launch_ns;       /* its batch was launched */
     uint64_t done_ns;         /* its read-back finished */
     uint64_t batch_id;
+    uint64_t png_bytes;       /* size of the PNG file (AXR_E_CAPACITY: it did not fit out_png) */
 } axr_server_result;
 
 typedef struct axr_server_stats {

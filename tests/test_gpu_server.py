@@ -125,3 +125,44 @@ def test_oversized_request_and_bad_arguments():
     with pytest.raises(AxrError):
         srv.wait(123456, 10)
     srv.close()
+
+
+@pytest.mark.parametrize("per_request", [0, 1])
+def test_png_outputs(ctx, per_request):
+    """Requests that ask for PNG files (RGB or RGBA) beside or instead of the raw planes, in
+    mixed batches: every file decodes to the request's colour plane; a buffer too small for
+    its file gives AXR_E_CAPACITY with the needed size."""
+    import pngfile
+
+    scenes = scenes_mix()
+    srv = api.Server(0, budget_bytes=2 << 30, max_batch=8, max_inflight=2, per_request=per_request)
+    ids = [srv.add_mesh(sc.mesh) for sc in scenes]
+    srv.hold(True)
+    pend = []
+    for k, sc in enumerate(scenes + scenes[:3]):
+        ch = (3, 4, 0)[k % 3]
+        bgra = np.zeros((sc.height, sc.width, 4), np.uint8)
+        png = np.zeros(api.png_bound(sc.width, sc.height, ch or 3), np.uint8) if ch else None
+        sh = sc.shader
+        b, g, r, a = sc.clear_bgra
+        t = srv.submit(ids[k % len(scenes)], api.Camera.from_workload(sc.camera),
+                       api.Shader(sh.kind, tuple(sh.light_direction), tuple(sh.light_color)), sc.width, sc.height,
+                       sc.model, (r, g, b, a), float("inf"), bgra, None, png_channels=ch, out_png=png)
+        pend.append((t, ch, bgra, png))
+    small = np.zeros(64, np.uint8)
+    sc = scenes[0]
+    t_small = srv.submit(ids[0], api.Camera.from_workload(sc.camera), api.BlinnPhongShader(), sc.width, sc.height,
+                         sc.model, png_channels=3, out_png=small)
+    srv.hold(False)
+    for t, ch, bgra, png in pend:
+        res = srv.wait(t, 60000)
+        assert res["status"] == AXR_OK
+        if ch:
+            data = png[: res["png_bytes"]].tobytes()
+            img, c, _ = pngfile.decode(data)
+            assert c == ch and np.array_equal(img, pngfile.expected(bgra, ch))
+        else:
+            assert res["png_bytes"] == 0
+    res = srv.wait(t_small, 60000)
+    assert res["status"] == 7 and res["png_bytes"] > 64  # AXR_E_CAPACITY
+    srv.close()
