@@ -177,6 +177,7 @@ SIGNATURES = {
     "axr_readback_destroy": (None, [P, P]),
     "axr_readback_start": (S, [P, P, C.c_int32, P, P, P]),
     "axr_readback_wait": (S, [P, P]),
+    "axr_readback_start_packed": (S, [P, P, C.c_int32, P, C.c_int32, P, C.c_uint64]),
     "axr_framebuffer_size": (S, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "axr_framebuffer_device_pointers": (S, [P, PP, PP]),
     "axr_camera_init": (S, [P, P, P, C.c_float, C.c_float]),

@@ -590,6 +590,12 @@ struct axr_readback {
     cudaStream_t copy[kStreams] = {};
     cudaEvent_t copied[kStreams] = {};
     cudaEvent_t ready = nullptr;  // the framebuffers are final (context stream)
+    // packed read-backs: the gathered planes on the device and the plane table
+    uint8_t* staging = nullptr;
+    size_t staging_cap = 0;
+    axr::PackedImage* images = nullptr;       // device
+    axr::PackedImage* images_host = nullptr;  // pinned
+    uint32_t images_cap = 0;
 };
 
 namespace {
@@ -603,6 +609,9 @@ void release_readback(axr_readback* rb) {
         if (rb->copied[k]) cudaEventDestroy(rb->copied[k]);
     }
     if (rb->ready) cudaEventDestroy(rb->ready);
+    dfree(rb->staging);
+    dfree(rb->images);
+    if (rb->images_host) cudaFreeHost(rb->images_host);
     delete rb;
 }
 
@@ -651,6 +660,69 @@ axr_status axr_readback_start(axr_context* ctx, axr_readback* rb, int32_t count,
         if (depth && depth[i]) AXR_CUDA(ctx, cudaMemcpyAsync(depth[i], fb->depth, n * 4, cudaMemcpyDeviceToHost, st));
     }
     for (int k = 0; k < axr_readback::kStreams; ++k) AXR_CUDA(ctx, cudaEventRecord(rb->copied[k], rb->copy[k]));
+    return AXR_OK;
+}
+
+axr_status axr_readback_start_packed(axr_context* ctx, axr_readback* rb, int32_t count,
+                                     const axr_framebuffer* const* fbs, int32_t format, uint8_t* host,
+                                     uint64_t capacity) {
+    if (!ctx || !rb || count < 0 || (count > 0 && (!fbs || !host))) return fail(ctx, AXR_E_INVALID, "bad read-back arguments");
+    if (format != AXR_PACKED_BGRA && format != AXR_PACKED_RGB) return fail(ctx, AXR_E_INVALID, "unknown format %d", format);
+    if (rb->device != ctx->device) return fail(ctx, AXR_E_INVALID, "the read-back belongs to another device");
+    const uint32_t bpp = format == AXR_PACKED_RGB ? 3u : 4u;
+    uint64_t bytes = 0, pixels = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        if (!fbs[i]) return fail(ctx, AXR_E_INVALID, "framebuffer %d is NULL", i);
+        pixels += (uint64_t)fbs[i]->width * fbs[i]->height;
+    }
+    bytes = pixels * bpp;
+    if (capacity < bytes)
+        return fail(ctx, AXR_E_INVALID, "the host buffer holds %llu bytes, the images need %llu",
+                    (unsigned long long)capacity, (unsigned long long)bytes);
+    if (count == 0) return AXR_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    // the previous read-back of this object has finished with its staging and table
+    for (int k = 0; k < axr_readback::kStreams; ++k) AXR_CUDA(ctx, cudaEventSynchronize(rb->copied[k]));
+    if (bytes > rb->staging_cap) {
+        dfree(rb->staging);
+        rb->staging = nullptr;
+        rb->staging_cap = 0;
+        AXR_CUDA(ctx, dmalloc(&rb->staging, (size_t)bytes));
+        rb->staging_cap = (size_t)bytes;
+    }
+    if ((uint32_t)count > rb->images_cap) {
+        dfree(rb->images);
+        rb->images = nullptr;
+        if (rb->images_host) cudaFreeHost(rb->images_host);
+        rb->images_host = nullptr;
+        rb->images_cap = 0;
+        AXR_CUDA(ctx, dmalloc(&rb->images, (size_t)count));
+        AXR_CUDA(ctx, cudaMallocHost(reinterpret_cast<void**>(&rb->images_host), sizeof(axr::PackedImage) * count));
+        rb->images_cap = (uint32_t)count;
+    }
+    uint64_t first = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const axr_framebuffer* fb = fbs[i];
+        rb->images_host[i] = axr::PackedImage{fb->color, first * bpp, (uint32_t)fb->width, (uint32_t)fb->height, first};
+        first += (uint64_t)fb->width * fb->height;
+    }
+    // gather on the context stream behind the frames, then the copies on the read-back's
+    // streams; later work on the context stream does not wait for the copies
+    AXR_CUDA(ctx, cudaMemcpyAsync(rb->images, rb->images_host, sizeof(axr::PackedImage) * count,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    AXR_CUDA(ctx, launch_packed(rb->images, (uint32_t)count, pixels, format == AXR_PACKED_RGB, rb->staging,
+                                ctx->cfg.num_sms, ctx->stream));
+    ctx->launches += 1;
+    AXR_CUDA(ctx, cudaEventRecord(rb->ready, ctx->stream));
+    const uint64_t part = (bytes + axr_readback::kStreams - 1) / axr_readback::kStreams;
+    for (int k = 0; k < axr_readback::kStreams; ++k) {
+        AXR_CUDA(ctx, cudaStreamWaitEvent(rb->copy[k], rb->ready, 0));
+        const uint64_t lo = std::min<uint64_t>(bytes, part * k), hi = std::min<uint64_t>(bytes, lo + part);
+        if (hi > lo)
+            AXR_CUDA(ctx, cudaMemcpyAsync(host + lo, rb->staging + lo, hi - lo, cudaMemcpyDeviceToHost, rb->copy[k]));
+        AXR_CUDA(ctx, cudaEventRecord(rb->copied[k], rb->copy[k]));
+    }
     return AXR_OK;
 }
 

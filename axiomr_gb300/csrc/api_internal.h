@@ -5,6 +5,16 @@
 
 #include "api_types.h"
 
+namespace axr {
+// One colour plane of a packed read-back (csrc/readback.cu).
+struct PackedImage {
+    const uint32_t* color;
+    unsigned long long out;    // byte offset of the image in the packed buffer
+    uint32_t width, height;
+    unsigned long long first;  // first pixel of the image in the call's pixel range
+};
+}
+
 namespace axr_internal {
 
 // Record a formatted message as the context's last error (or the thread's, without a
@@ -26,6 +36,11 @@ void free_batch_staging(axr_batch* b);
 // holds ctx->mu; axr_batch_create / axr_batch_launch without the locking).
 axr_status batch_plan(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch* b, bool async);
 axr_status batch_launch(axr_context* ctx, const axr_batch* b);
+// The gather of colour planes behind axr_readback_start_packed (csrc/readback.cu):
+// `images_dev` (device) lists each plane, its byte offset in dst and its first pixel in
+// the call's range of `pixels`; rgb: RGB8 top row first, else BGRA8 as stored.
+cudaError_t launch_packed(const axr::PackedImage* images_dev, uint32_t count, unsigned long long pixels, bool rgb,
+                          uint8_t* dst, int num_sms, cudaStream_t stream);
 // Release the PNG encoder's scratch (the caller synchronises first).
 void free_png(axr_context* ctx);
 // PNG batches for the serving loop, without blocking: create / release; enqueue an encode

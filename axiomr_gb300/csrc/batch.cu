@@ -196,12 +196,21 @@ __device__ uint32_t tile_scan(const DrawParams& p, const UnitInfo& ui, const Til
     const float cd = ui.clear_depth;
     const uint32_t cc = ui.clear_bgra;
     uint32_t nwin = 0, nclip = 0;
+    // all eight keys first: the resets below would otherwise keep the compiler from
+    // issuing a row's load before the previous row's store (one load in flight)
+    unsigned long long keys[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int py = c.ty * kTile + ly0 + 2 * r;
+        const bool in = px < t.width && py < t.height;
+        keys[r] = (dirty && in) ? __ldcg(t.key + (size_t)py * (size_t)t.width + (size_t)px) : kEmptyKey;
+    }
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
         const int ly = ly0 + 2 * r, py = c.ty * kTile + ly, pix = ly * kTile + lx;
         const bool in = px < t.width && py < t.height;
         const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
-        const unsigned long long key = (dirty && in) ? t.key[idx] : kEmptyKey;
+        const unsigned long long key = keys[r];
         const bool has = key != kEmptyKey;
         const bool clipped = has && (((uint32_t)key) & 8u) != 0u;
         const unsigned mw = __ballot_sync(0xFFFFFFFFu, has && !clipped);

@@ -172,6 +172,10 @@ __device__ __forceinline__ f3 fresnel_schlick(float cos_theta, f3 f0) {
 
 __device__ __forceinline__ f3 pow3(f3 b, f3 e) { return mk3(powf(b.x, e.x), powf(b.y, e.y), powf(b.z, e.z)); }
 
+// powf(b, e) for b = max(x, 0): pow(+0, e) is +0 for every e > 0, so that case skips the
+// call (same bits; warps whose pixels all face away from the light skip it entirely).
+__device__ __forceinline__ float pow_clamped(float b, float e) { return (b == 0.0f && e > 0.0f) ? 0.0f : powf(b, e); }
+
 template <int S>
 __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMaterial& m, f3 w, const VSOut* t) {
     if constexpr (S == kFlat) {
@@ -197,7 +201,7 @@ __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMat
         float diff = smax(dot(normal, light_dir), 0.0f);
         f3 diffuse = mul(diff, lc);
         f3 refl = reflect(neg(light_dir), normal);
-        float spec = powf(smax(dot(view_dir, refl), 0.0f), fmul(m.specular_exponent, 50.0f));
+        float spec = pow_clamped(smax(dot(view_dir, refl), 0.0f), fmul(m.specular_exponent, 50.0f));
         f3 specular = mul(fmul(0.5f, spec), lc);
         f3 c = mul(add(add(ambient, diffuse), specular), xyz(albedo));
         return mk4(c.x, c.y, c.z, 1.0f);
@@ -262,7 +266,7 @@ __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMat
         f3 ambient = mul(0.1f, lc);
         float diff = smax(dot(n, light_dir), 0.0f);
         f3 diffuse = mul(diff, lc);
-        float spec = powf(smax(dot(n, halfway), 0.0f), fmul(m.specular_exponent, 50.0f));
+        float spec = pow_clamped(smax(dot(n, halfway), 0.0f), fmul(m.specular_exponent, 50.0f));
         f3 specular = mul(fmul(0.5f, spec), lc);
         f3 c = mul(add(add(ambient, diffuse), specular), albedo);
         return mk4(c.x, c.y, c.z, 1.0f);

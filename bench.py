@@ -707,27 +707,48 @@ def run_batch(args, dist: Dist):
         api.check(lib.axr_readback_create(ctx.handle, C.byref(h)), ctx.handle)
         rbs.append(h)
 
-    def pipelined(steps):
+    # the packed read-back: all planes gathered on the device, one block per step into one
+    # pinned buffer per set (BGRA as stored, or RGB top row first as the window shows them)
+    pixels = sum(d.framebuffer.width * d.framebuffer.height for d in draws)
+    packed = {fmt: [pinned_bytes(lib, pixels * bpp, keep) for _ in sets] for fmt, bpp in ((0, 4), (1, 3))}
+
+    def start_planes(cur):
+        api.check(lib.axr_readback_start(ctx.handle, rbs[cur], n, fb_arrs[cur], bgra_arrs[cur], None), ctx.handle)
+
+    def start_packed(fmt):
+        def start(cur):
+            buf = packed[fmt][cur]
+            api.check(lib.axr_readback_start_packed(ctx.handle, rbs[cur], n, fb_arrs[cur], fmt, buf.ctypes.data,
+                                                    buf.nbytes), ctx.handle)
+        return start
+
+    def pipelined(steps, start):
         for k in range(steps):
             cur = k % 2
             api.draw_batch(ctx, tables[cur])
-            api.check(lib.axr_readback_start(ctx.handle, rbs[cur], n, fb_arrs[cur], bgra_arrs[cur], None), ctx.handle)
+            start(cur)
             if k:
                 api.check(lib.axr_readback_wait(ctx.handle, rbs[1 - cur]), ctx.handle)
         api.check(lib.axr_readback_wait(ctx.handle, rbs[(steps - 1) % 2]), ctx.handle)
 
-    pipelined(4)
-    torch.cuda.synchronize()
     e2e_steps = max(3, args.steps // 2)
+
+    def timed_pipeline(start):
+        pipelined(4, start)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        e0.record(stream)
+        pipelined(e2e_steps, start)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return n * e2e_steps * dist.world / (dist.max(float(e0.elapsed_time(e1))) / 1e3)
+
     l0 = ctx.profile()["kernel_launches"]
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    dist.barrier()
-    e0.record(stream)
-    pipelined(e2e_steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_launches = (ctx.profile()["kernel_launches"] - l0) / e2e_steps
-    e2e_value = n * e2e_steps * dist.world / (dist.max(float(e0.elapsed_time(e1))) / 1e3)
+    e2e_value = timed_pipeline(start_packed(0))
+    e2e_launches = (ctx.profile()["kernel_launches"] - l0) / (e2e_steps + 4)
+    planes_value = timed_pipeline(start_planes)
+    rgb_value = timed_pipeline(start_packed(1))
     for h in rbs:
         lib.axr_readback_destroy(ctx.handle, h)
 
@@ -792,13 +813,20 @@ def run_batch(args, dist: Dist):
         "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "path": "per step axr_draw_batch (draw table from the host) + read-back of all 512 rendered "
-                        "images (BGRA8 colour planes) into pinned memory on 4 copy streams (axr_readback_start / "
-                        "axr_readback_wait), pipelined over two framebuffer sets so that step k's copies overlap "
-                        "step k+1's rendering; meshes and textures resident; inputs larger than L2",
+                        "images (BGRA8 colour planes, as stored) into one pinned buffer: gathered on the device "
+                        "and copied as one block (axr_readback_start_packed / axr_readback_wait), pipelined over "
+                        "two framebuffer sets so that step k's copies overlap step k+1's rendering; meshes and "
+                        "textures resident; inputs larger than L2",
                 "steps": e2e_steps, "gpu_launches_per_step": e2e_launches,
+                "per_plane_copies": {"value": round(planes_value, 2), "unit": "frames/s",
+                                     "path": "the same with one copy per colour plane (axr_readback_start)"},
                 "serial": {"value": round(serial_value, 2), "unit": "frames/s",
                            "path": "the same without overlap: draw, read back (axr_framebuffers_read_async), "
                                    "next step; L2 flushed before each step"}},
+        "e2e_rgb": {"value": round(rgb_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(3 * pixels),
+                    "path": "the e2e pipeline with the frames as RGB8, top row first (the picture the reference's "
+                            "window shows), packed on the device: 3 bytes per pixel cross the link"},
         "e2e_png": png,
         "gpu_launches": int(info["launches"]) * len(step_ms),
         "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),

@@ -204,6 +204,17 @@ void axr_readback_destroy(axr_context* ctx, axr_readback* rb);
 axr_status axr_readback_start(axr_context* ctx, axr_readback* rb, int32_t count, const axr_framebuffer* const* fbs,
                               uint8_t* const* bgra, float* const* depth);
 axr_status axr_readback_wait(axr_context* ctx, axr_readback* rb);
+/* A packed read-back: the colour planes of `count` framebuffers gathered on the device and
+ * copied as one block into `host` (capacity bytes), image after image: AXR_PACKED_BGRA the
+ * planes as stored (4 bytes per pixel, framebuffer row 0 first), AXR_PACKED_RGB 3 bytes per
+ * pixel with the top row first: the picture the reference's window shows (Window::present,
+ * src/window.cpp:70-84). Image i starts at bytes-per-pixel * (pixels of images 0..i-1).
+ * Later work on the context stream does not wait for it; axr_readback_wait does. */
+#define AXR_PACKED_BGRA 0
+#define AXR_PACKED_RGB 1
+axr_status axr_readback_start_packed(axr_context* ctx, axr_readback* rb, int32_t count,
+                                     const axr_framebuffer* const* fbs, int32_t format, uint8_t* host,
+                                     uint64_t capacity);
 /* Upload host colour and/or depth into the framebuffer (either may be NULL). */
 axr_status axr_framebuffer_write(axr_context* ctx, axr_framebuffer* fb, const uint8_t* bgra, const float* depth);
 axr_status axr_framebuffer_size(const axr_framebuffer* fb, int32_t* width, int32_t* height);

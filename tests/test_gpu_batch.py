@@ -258,3 +258,35 @@ def test_detached_readback_pipeline(ctx):
             assert np.array_equal(got, want)
     for h in rbs:
         ctx.lib.axr_readback_destroy(ctx.handle, h)
+
+
+def test_packed_readback_formats(ctx):
+    """axr_readback_start_packed: all colour planes in one host buffer, image after image,
+    as stored (BGRA, row 0 first) or as the window shows them (RGB, top row first)."""
+    import ctypes as C
+
+    scenes = small_batch(count=5, seed=29)
+    draws = api.batch_draws(ctx, scenes)
+    api.draw_batch(ctx, draws)
+    planes = [d.framebuffer.read()[0] for d in draws]
+    n = len(draws)
+    fbs = (C.c_void_p * n)(*[d.framebuffer.handle.value for d in draws])
+    h = C.c_void_p()
+    api.check(ctx.lib.axr_readback_create(ctx.handle, C.byref(h)), ctx.handle)
+    pixels = sum(p.shape[0] * p.shape[1] for p in planes)
+    for fmt, bpp in ((0, 4), (1, 3)):
+        buf = np.zeros(pixels * bpp + 7, np.uint8)
+        api.check(ctx.lib.axr_readback_start_packed(ctx.handle, h, n, fbs, fmt, buf.ctypes.data, buf.nbytes),
+                  ctx.handle)
+        api.check(ctx.lib.axr_readback_wait(ctx.handle, h), ctx.handle)
+        at = 0
+        for p in planes:
+            k = p.shape[0] * p.shape[1] * bpp
+            img = buf[at:at + k].reshape(p.shape[0], p.shape[1], bpp)
+            want = p if fmt == 0 else p[::-1][:, :, [2, 1, 0]]
+            assert np.array_equal(img, want)
+            at += k
+        assert not buf[at:].any()
+    small = np.zeros(16, np.uint8)
+    assert ctx.lib.axr_readback_start_packed(ctx.handle, h, n, fbs, 1, small.ctypes.data, small.nbytes) != 0
+    ctx.lib.axr_readback_destroy(ctx.handle, h)
