@@ -19,6 +19,7 @@
 // never throws. Every object holds the context it was created on.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <limits>
@@ -148,6 +149,18 @@ public:
     }
     // BGRA bytes (width*height*4) and depth (width*height) into host memory; blocks.
     void read(uint8_t* bgra, float* depth) const { check(axr_framebuffer_read(ctx_.get(), fb_.get(), bgra, depth), ctx_.get()); }
+    // The colour plane as a PNG file (RGB, top row first: what the reference's window shows;
+    // channels 4 = RGBA), encoded on the GPU.
+    std::vector<uint8_t> readPng(uint32_t channels = 3) const {
+        std::vector<uint8_t> file(axr_png_bound(uint32_t(width_), uint32_t(height_), channels));
+        const axr_framebuffer* f = fb_.get();
+        void* out = file.data();
+        const uint64_t cap = file.size();
+        uint64_t size = 0;
+        check(axr_framebuffers_read_png(ctx_.get(), 1, &f, channels, &out, &cap, &size), ctx_.get());
+        file.resize(size_t(size));
+        return file;
+    }
     uint32_t getWidth() const { return uint32_t(width_); }
     uint32_t getHeight() const { return uint32_t(height_); }
     axr_framebuffer* get() const { return fb_.get(); }
@@ -158,34 +171,56 @@ private:
     std::shared_ptr<axr_framebuffer> fb_;
 };
 
-// Camera (reference include/camera.hpp): matrices of Camera(position, target, fov,
-// aspect) after update(0), near 0.1, far 100.
+// Camera (reference include/camera.hpp, src/camera.cpp) on the library's camera state: the
+// reference's setters, handleInput and update(deltaTime), bit for bit. The constructor
+// also runs update(0), as a frame loop does before its first frame (the reference
+// constructor leaves the view matrix at identity until an update).
+struct InputState {  // what Camera::handleInput reads from the Window
+    float mouseX = 0, mouseY = 0;
+    bool rightButton = false;
+    std::array<bool, 256> keys{};  // indexed by the key's character ('W', 'A', 'S', 'D')
+};
+
 class Camera {
 public:
     Camera(std::array<float, 3> position = {0, 0, 0}, std::array<float, 3> target = {0, 0, -1}, float fov = 60.0f,
-           float aspectRatio = 16.0f / 9.0f)
-        : position_(position) {
-        check(axr_camera_matrices(position.data(), target.data(), fov, aspectRatio, view_.data(), proj_.data(),
-                                  viewProj_.data()));
-        setViewport(0, 0, 800, 600);
+           float aspectRatio = 16.0f / 9.0f) {
+        check(axr_camera_init(&s_, position.data(), target.data(), fov, aspectRatio));
+        update(0.0f);
     }
-    void setViewport(int x, int y, int width, int height) { check(axr_viewport_matrix(x, y, width, height, viewport_.data())); }
-    const Mat4& getViewMatrix() const { return view_; }
-    const Mat4& getProjectionMatrix() const { return proj_; }
-    const Mat4& getViewProjectionMatrix() const { return viewProj_; }
-    const Mat4& getViewportMatrix() const { return viewport_; }
-    std::array<float, 3> getPosition() const { return position_; }
+    void setPosition(std::array<float, 3> p) { check(axr_camera_set_position(&s_, p.data())); }
+    void setTarget(std::array<float, 3> t) { check(axr_camera_set_target(&s_, t.data())); }
+    void setFov(float fov) { check(axr_camera_set_fov(&s_, fov)); }
+    void setAspectRatio(float a) { check(axr_camera_set_aspect_ratio(&s_, a)); }
+    void setViewport(int x, int y, int width, int height) { check(axr_camera_set_viewport(&s_, x, y, width, height)); }
+    void handleInput(const InputState& in) {
+        axr_input_state st{};
+        st.mouse[0] = in.mouseX;
+        st.mouse[1] = in.mouseY;
+        st.mouse_buttons[1] = in.rightButton ? 1 : 0;
+        for (int k = 0; k < 256; ++k) st.keys[k] = in.keys[size_t(k)] ? 1 : 0;
+        check(axr_camera_handle_input(&s_, &st));
+    }
+    void update(float deltaTime) { check(axr_camera_update(&s_, deltaTime)); }
+    Mat4 getViewMatrix() const { return to_mat(s_.view); }
+    Mat4 getProjectionMatrix() const { return to_mat(s_.projection); }
+    Mat4 getViewProjectionMatrix() const { return to_mat(s_.view_proj); }
+    Mat4 getViewportMatrix() const { return to_mat(desc().viewport); }
+    std::array<float, 3> getPosition() const { return {s_.position[0], s_.position[1], s_.position[2]}; }
     axr_camera_desc desc() const {
         axr_camera_desc d{};
-        std::copy(viewProj_.begin(), viewProj_.end(), d.view_proj);
-        std::copy(viewport_.begin(), viewport_.end(), d.viewport);
-        std::copy(position_.begin(), position_.end(), d.position);
+        check(axr_camera_describe(&s_, &d));
         return d;
     }
+    const axr_camera_state& state() const { return s_; }
 
 private:
-    std::array<float, 3> position_;
-    Mat4 view_{}, proj_{}, viewProj_{}, viewport_{};
+    static Mat4 to_mat(const float* m) {
+        Mat4 r{};
+        std::copy(m, m + 16, r.begin());
+        return r;
+    }
+    axr_camera_state s_{};
 };
 
 // Shaders (reference include/shaders/shaders.hpp) as descriptors.

@@ -56,3 +56,37 @@ def test_facade_renders_like_oracle(tmp_path, port):
     depth = np.frombuffer(raw[4 * n:], np.float32).reshape(sc.height, sc.width)
     exp = port.render(sc)[:2]
     assert_parity((bgra, depth), exp, "C++ facade")
+
+
+def test_facade_camera_matches_reference_fixture(tmp_path):
+    """The camera behind axr::Camera (axr_camera_*), driven from C++, reproduces the
+    reference Camera's matrices after every operation of the fixture scripts; the facade
+    class itself equals the Python binding's camera."""
+    import camscript
+    from axiomr_gb300 import api, build
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    lib = build.build()
+    exe = tmp_path / "facade_camera"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", f"-I{ROOT / 'include'}",
+                    str(ROOT / "tests" / "cpp" / "facade_camera.cpp"), "-o", str(exe), f"-L{lib.parent}", "-laxr",
+                    f"-Wl,-rpath,{lib.parent}"], check=True)
+    z = np.load(ROOT / "tests" / "golden" / "camera_scripts.npz")
+    for k, (pos, tgt, fov, aspect) in enumerate(camscript.STARTS):
+        ops = z[f"ops_{k}"]
+        script = tmp_path / f"s{k}.bin"
+        with open(script, "wb") as f:
+            f.write(np.asarray([*pos, *tgt, fov, aspect], np.float32).tobytes())
+            f.write(struct.pack("<I", ops.shape[0]))
+            f.write(np.ascontiguousarray(ops, np.float32).tobytes())
+        out = tmp_path / f"o{k}.bin"
+        subprocess.run([str(exe), str(script), str(out)], check=True)
+        got = np.fromfile(out, np.float32)
+        n = ops.shape[0]
+        assert np.array_equal(got[: 51 * n].reshape(n, 51).view(np.uint32), z[f"out_{k}"].view(np.uint32)), k
+        cam = api.Camera(pos, tgt, fov, aspect)
+        cam.handleInput((10.0, 10.0), True)
+        cam.handleInput((40.0, 25.0), True, "W")
+        cam.update(0.1)
+        assert np.array_equal(got[51 * n:].view(np.uint32), cam.view_proj.view(np.uint32)), k
