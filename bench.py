@@ -614,9 +614,11 @@ def run_batch(args, dist: Dist):
     tuning = ctx.tuning() if args.no_autotune else api.autotune(ctx, draws, repeats=2)
     batch = api.Batch(ctx, draws)
     info = batch.info()
+    k0 = ctx.profile()["kernel_launches"]
     graph = api.Graph(ctx).begin()
     batch.launch()
     graph.end()
+    kernels_per_step = ctx.profile()["kernel_launches"] - k0  # the kernels one replay runs
 
     # ---- plain per-draw path, recorded once into a graph as well
     ctx.reserve(max(int(sc.mesh.indices.shape[0]) for sc in scenes))
@@ -828,7 +830,7 @@ def run_batch(args, dist: Dist):
                     "path": "the e2e pipeline with the frames as RGB8, top row first (the picture the reference's "
                             "window shows), packed on the device: 3 bytes per pixel cross the link"},
         "e2e_png": png,
-        "gpu_launches": int(info["launches"]) * len(step_ms),
+        "gpu_launches": int(kernels_per_step) * len(step_ms),
         "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),
                      "peak": hbm_peak, "peak_source": peak_kind, "unit": "GB/s",
                      "frac": round(dom_achieved / hbm_peak, 4), "traffic": profiled_traffic(kernel_of[dom], "batch"),
