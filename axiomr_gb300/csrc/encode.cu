@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "api_internal.h"
@@ -782,6 +783,7 @@ struct PngState {
     cudaEvent_t tables_free[2] = {};
     int next = 0;
     axr_png_batch* readback = nullptr;  // axr_framebuffers_read_png
+    std::mutex readback_mu;             // held for a whole axr_framebuffers_read_png call
 };
 
 void free_png(axr_context* ctx) {
@@ -1188,10 +1190,17 @@ extern "C" axr_status axr_framebuffers_read_png(axr_context* ctx, int32_t count,
     if (channels != 3 && channels != 4) return fail(ctx, AXR_E_INVALID, "channels must be 3 (RGB) or 4 (RGBA)");
     if (count == 0) return AXR_OK;
     axr_png_batch* b;
+    PngState* ps;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if (!ctx->png) ctx->png = new PngState();
+        ps = ctx->png;
+    }
+    // the internal batch serves one call at a time (lock order: readback_mu, then ctx->mu)
+    std::lock_guard<std::mutex> whole(ps->readback_mu);
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
         DeviceGuard g(ctx->device);
-        if (!ctx->png) ctx->png = new PngState();
         if (!ctx->png->readback) {
             axr_status st = create_batch(ctx, &ctx->png->readback);
             if (st != AXR_OK) return st;

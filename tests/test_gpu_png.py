@@ -181,3 +181,31 @@ def test_png_batch_pipeline(ctx):
         check_file(data, im, 3)
     pa.close()
     pb.close()
+
+
+def test_read_png_from_two_threads(ctx):
+    """Calls on one context from two threads are serialised: each gets its own files."""
+    import threading
+
+    rng = np.random.default_rng(31)
+    sets = [[rng.integers(0, 256, (40 + 7 * k, 60, 4), dtype=np.uint8) for k in range(6)] for _ in range(2)]
+    fbs = [[fb_with(ctx, im) for im in s] for s in sets]
+    out = [None, None]
+    errors = []
+
+    def run(i):
+        try:
+            for _ in range(5):
+                out[i] = api.read_png(ctx, fbs[i], 3)
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(e)
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
+    for i in range(2):
+        for im, data in zip(sets[i], out[i]):
+            check_file(data, im, 3)
