@@ -284,6 +284,8 @@ void axr_context_destroy(axr_context* ctx) {
     delete ctx;
 }
 
+int32_t axr_abi_version(void) { return AXR_ABI_VERSION; }
+
 const char* axr_last_error(const axr_context* ctx) { return ctx ? ctx->error.c_str() : g_no_ctx_error.c_str(); }
 
 void* axr_context_stream(axr_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }

@@ -25,7 +25,10 @@
 extern "C" {
 #endif
 
-#define AXR_ABI_VERSION 1
+/* Raised whenever a struct or signature of this header changes; a program built against
+ * this header can compare it with axr_abi_version() of the library it loaded. */
+#define AXR_ABI_VERSION 2
+int32_t axr_abi_version(void);
 
 /* The reference reports failures with exceptions or silently (src/tiled_pipeline.cpp:146,
  * 126; include/thread_pool.hpp:23-24); across a C ABI they become status codes, with a

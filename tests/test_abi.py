@@ -86,3 +86,14 @@ def test_context_create_reports_missing_gpu():
     assert h.value is None
     assert lib.axr_last_error(None)
     del n
+
+
+def test_abi_version_matches_header():
+    import re
+    from pathlib import Path
+
+    from axiomr_gb300 import _lib
+
+    hdr = (Path(__file__).resolve().parent.parent / "include" / "axr.h").read_text()
+    want = int(re.search(r"#define AXR_ABI_VERSION (\d+)", hdr).group(1))
+    assert _lib.load().axr_abi_version() == want
