@@ -181,6 +181,7 @@ SIGNATURES = {
     "axr_framebuffer_size": (S, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "axr_framebuffer_device_pointers": (S, [P, PP, PP]),
     "axr_abi_version": (C.c_int32, []),
+    "axr_diag_barrier_timeout": (S, [P, C.c_uint32]),
     "axr_camera_init": (S, [P, P, P, C.c_float, C.c_float]),
     "axr_camera_set_position": (S, [P, P]),
     "axr_camera_set_target": (S, [P, P]),

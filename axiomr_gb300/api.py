@@ -27,6 +27,7 @@ from ._lib import (AXR_DRAW_CLEAR_COLOR, AXR_DRAW_CLEAR_DEPTH, AXR_TUNE_CLASSES,
                    DrawDesc, DrawStats, GroupDesc, MaterialDesc, MeshDesc, ShaderDesc, check)
 
 FLAT, PHONG, PBR, BLINN_PHONG, GOURAUD = 0, 1, 2, 3, 4
+BATCH_PERSISTENT, BATCH_PHASED = 0, 1  # launch forms of the batched kernel (AXR_BATCH_*)
 
 
 def _f32(a) -> np.ndarray:

@@ -21,6 +21,7 @@ using namespace axr;
 
 #include "api_types.h"
 #include "api_internal.h"
+#include "batch.h"
 
 namespace axr_internal {
 
@@ -285,6 +286,17 @@ void axr_context_destroy(axr_context* ctx) {
 }
 
 int32_t axr_abi_version(void) { return AXR_ABI_VERSION; }
+
+axr_status axr_diag_barrier_timeout(axr_context* ctx, uint32_t timeout_ms) {
+    if (!ctx || timeout_ms == 0 || timeout_ms > 10000) return fail(ctx, AXR_E_INVALID, "timeout_ms must be 1..10000");
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        DeviceGuard g(ctx->device);
+        AXR_CUDA(ctx, launch_barrier_probe(ctx->counters, (unsigned long long)timeout_ms * 1000000ull, ctx->stream));
+        ctx->launches += 1;
+    }
+    return axr_sync(ctx);
+}
 
 const char* axr_last_error(const axr_context* ctx) { return ctx ? ctx->error.c_str() : g_no_ctx_error.c_str(); }
 

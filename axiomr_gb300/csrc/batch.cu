@@ -56,9 +56,11 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 }
 
 // Grid-wide barrier of the cooperative launch (all CTAs are co-resident). The wait is
-// bounded: after kBarrierTimeoutNs it sets kErrBarrier and the CTA leaves the kernel.
+// bounded: after timeout_ns (kBarrierTimeoutNs unless a caller passes less) it sets
+// kErrBarrier and returns false, and the CTA leaves the kernel.
 // With phase timing on, the last CTA to arrive at barrier k records the time.
-__device__ bool grid_barrier(DevCounters* c, BatchProfile* prof, int k) {
+__device__ bool grid_barrier(DevCounters* c, BatchProfile* prof, int k,
+                             unsigned long long timeout_ns = kBarrierTimeoutNs) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -73,7 +75,7 @@ __device__ bool grid_barrier(DevCounters* c, BatchProfile* prof, int k) {
         } else {
             const unsigned long long t0 = global_ns();
             while (ld_acquire(&c->bar_gen) == gen) {
-                if (global_ns() - t0 > kBarrierTimeoutNs) {
+                if (global_ns() - t0 > timeout_ns) {
                     atomicOr(&c->error, kErrBarrier);
                     ok = 0;
                     break;
@@ -611,6 +613,13 @@ __global__ void __launch_bounds__(kBatchBlock) batch_clear_kernel(const __grid_c
     }
 }
 
+// Failure-path probe: CTA 0 waits at a grid barrier that CTA 1 never reaches, so the
+// bounded wait gives up after timeout_ns and sets kErrBarrier.
+__global__ void barrier_probe_kernel(DevCounters* c, unsigned long long timeout_ns) {
+    if (blockIdx.x != 0) return;
+    grid_barrier(c, nullptr, 0, timeout_ns);
+}
+
 template <int S>
 cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, cudaEvent_t* ev,
                            uint64_t* launches) {
@@ -682,6 +691,13 @@ cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sm
         case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_barrier_probe(DevCounters* counters, unsigned long long timeout_ns, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(counters, 0, kBatchCountersReset, stream);
+    if (e != cudaSuccess) return e;
+    barrier_probe_kernel<<<2, 32, 0, stream>>>(counters, timeout_ns);
+    return cudaGetLastError();
 }
 
 }  // namespace axr

@@ -17,4 +17,8 @@ namespace axr {
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
                          cudaEvent_t* phase_events, uint64_t* launches);
 
+// Failure-path probe of the grid barrier: one CTA waits at a barrier the other never
+// reaches; the bounded wait gives up after timeout_ns and sets the barrier error bit.
+cudaError_t launch_barrier_probe(DevCounters* counters, unsigned long long timeout_ns, cudaStream_t stream);
+
 }  // namespace axr

@@ -77,6 +77,11 @@ void* axr_context_stream(axr_context* ctx);
 axr_status axr_context_set_stream(axr_context* ctx, void* stream);
 /* Wait for all work enqueued on the context's stream; reports device-side errors. */
 axr_status axr_sync(axr_context* ctx);
+/* Diagnostic of the failure path of the batched kernel's grid barrier (no reference
+ * counterpart): one CTA waits at a barrier that the other CTA never reaches, the bounded
+ * wait gives up after timeout_ms (1..10000), and the call returns what axr_sync reports,
+ * AXR_E_TIMEOUT; the context stays usable. No GPU fault is involved. */
+axr_status axr_diag_barrier_timeout(axr_context* ctx, uint32_t timeout_ms);
 /* Pre-size the scratch arena for draws of up to max_faces faces (needed before a draw
  * is captured into a CUDA graph; draws outside a capture grow it on demand). */
 axr_status axr_reserve(axr_context* ctx, uint32_t max_faces);

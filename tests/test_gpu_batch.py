@@ -290,3 +290,33 @@ def test_packed_readback_formats(ctx):
     small = np.zeros(16, np.uint8)
     assert ctx.lib.axr_readback_start_packed(ctx.handle, h, n, fbs, 1, small.ctypes.data, small.nbytes) != 0
     ctx.lib.axr_readback_destroy(ctx.handle, h)
+
+
+def test_grid_barrier_timeout_reports_and_context_survives(ctx):
+    """Failure path of the persistent form's grid barrier, without a GPU fault: one CTA waits
+    at a barrier the other never reaches; the bounded wait gives up after 50 ms, the next
+    sync reports AXR_E_TIMEOUT, and the same context then renders a persistent batch that
+    equals the phased one."""
+    import time
+
+    t0 = time.perf_counter()
+    st = int(ctx.lib.axr_diag_barrier_timeout(ctx.handle, 50))
+    took = time.perf_counter() - t0
+    assert st == 4, (st, ctx.lib.axr_last_error(ctx.handle))
+    assert 0.04 < took < 5.0
+    assert int(ctx.lib.axr_diag_barrier_timeout(ctx.handle, 0)) == 1  # argument check
+    ctx.sync()  # the error bit was cleared by the report
+    scenes = small_batch(count=8, seed=23)
+    frames = {}
+    saved = ctx.batch_form
+    try:
+        for form in (api.BATCH_PERSISTENT, api.BATCH_PHASED):
+            ctx.batch_form = form
+            draws = api.batch_draws(ctx, scenes)
+            api.draw_batch(ctx, draws)
+            ctx.sync()
+            frames[form] = [d.framebuffer.read() for d in draws]
+    finally:
+        ctx.batch_form = saved
+    for k in range(len(scenes)):
+        assert_same(frames[api.BATCH_PERSISTENT][k], frames[api.BATCH_PHASED][k], f"draw {k} after the timeout")
