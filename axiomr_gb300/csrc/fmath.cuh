@@ -71,6 +71,33 @@ __device__ __forceinline__ f4 add(f4 a, f4 b) {
 __device__ __forceinline__ f4 mul(f4 a, float s) { return {fmul(a.x, s), fmul(a.y, s), fmul(a.z, s), fmul(a.w, s)}; }
 __device__ __forceinline__ f4 mix(f4 x, f4 y, float a) { return add(mul(x, fsub(1.0f, a)), mul(y, a)); }
 
+// Colour-only math: for lighting terms that reach the framebuffer only through the 8-bit
+// quantisation (never coverage, depth or a texture coordinate). Each result carries a
+// relative error of a few 1e-7 at most, far inside the 1 LSB colour tolerance, at a
+// fraction of the cost of the correctly rounded sequences:
+//   crcp(x)        rcp.approx.f32 (max 1 ulp over the full range, subnormals kept):
+//                  0 -> inf, inf -> 0, NaN -> NaN, as 1/x
+//   cdiv(a, b)     a * crcp(b): the IEEE special cases of a/b (0/0, inf/inf -> NaN)
+//   cnormalize(v)  v * rsqrtf(v.v): scales v without turning it, so the direction is the
+//                  exact one; zero vectors give NaN as 1/sqrt(0) does
+//   cpow(b, e)     exp2f(e * log2f(b)) for b >= 0: relative error about
+//                  ln2 * |e log2 b| * 2^-23 + 2 ulp, which stays near 1e-6 wherever the
+//                  power is large enough to move an 8-bit channel, for any exponent;
+//                  as powf: e = 0 or b = 1 gives 1, b = 0 gives 0 (e > 0) or inf
+//                  (e < 0), b < 0 (non-integer e) or NaN gives NaN
+__device__ __forceinline__ float crcp(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float cdiv(float a, float b) { return fmul(a, crcp(b)); }
+__device__ __forceinline__ f3 cdiv(f3 a, f3 b) { return {cdiv(a.x, b.x), cdiv(a.y, b.y), cdiv(a.z, b.z)}; }
+__device__ __forceinline__ f3 cdivs(f3 a, float s) { return mul(a, crcp(s)); }
+__device__ __forceinline__ f3 cnormalize(f3 v) { return mul(v, rsqrtf(dot(v, v))); }
+__device__ __forceinline__ float cpow(float b, float e) {
+    return (e == 0.0f || b == 1.0f) ? 1.0f : exp2f(fmul(e, log2f(b)));
+}
+
 // Column-major 4x4 (m[4*col + row]) times (x, y, z, w): pairwise sum of the four columns.
 __device__ __forceinline__ f4 mat4_mul(const float* m, float x, float y, float z, float w) {
     f4 c0 = mk4(m[0], m[1], m[2], m[3]), c1 = mk4(m[4], m[5], m[6], m[7]);

@@ -9,9 +9,15 @@
 //                     with the half vector H = normalize(L + V) and no normal map
 //   Gouraud           this project's shader: RGB carried in Vertex::normal, A in uv.x
 // Texture coordinates and barycentric interpolation use the exact-rounding helpers, so
-// the texel a fragment reads is the reference's. powf comes from the CUDA math library,
-// whose last-bit differences from the host's powf stay inside the 1 LSB colour
-// tolerance after 8-bit quantisation.
+// the texel a fragment reads is the reference's. The lighting terms after that reach the
+// framebuffer only through the 8-bit quantisation: their divisions and powers use the
+// colour-only helpers of fmath.cuh (relative error of a few 1e-7 on exact inputs, not
+// amplified by what follows), inside the 1 LSB colour tolerance. Normalisation stays
+// correctly rounded wherever the vector feeds a specular term: a sharp highlight
+// (PBR's distribution term at low roughness, a large Phong exponent) would magnify a
+// 1e-7 change in n.h far beyond 1 LSB. Only Flat's normal, which feeds a clamped dot
+// product alone, uses the fast form. Products and sums keep the reference's order and
+// rounding.
 #pragma once
 #include "device_types.h"
 #include "fmath.cuh"
@@ -170,16 +176,16 @@ __device__ __forceinline__ f3 fresnel_schlick(float cos_theta, f3 f0) {
     return add(f0, mul(sub(mk3(1.f, 1.f, 1.f), f0), term));
 }
 
-__device__ __forceinline__ f3 pow3(f3 b, f3 e) { return mk3(powf(b.x, e.x), powf(b.y, e.y), powf(b.z, e.z)); }
+__device__ __forceinline__ f3 pow3(f3 b, f3 e) { return mk3(cpow(b.x, e.x), cpow(b.y, e.y), cpow(b.z, e.z)); }
 
-// powf(b, e) for b = max(x, 0): pow(+0, e) is +0 for every e > 0, so that case skips the
-// call (same bits; warps whose pixels all face away from the light skip it entirely).
-__device__ __forceinline__ float pow_clamped(float b, float e) { return (b == 0.0f && e > 0.0f) ? 0.0f : powf(b, e); }
+// pow(b, e) for b = max(x, 0): pow(+0, e) is +0 for every e > 0, so that case skips the
+// call (warps whose pixels all face away from the light skip it entirely).
+__device__ __forceinline__ float pow_clamped(float b, float e) { return (b == 0.0f && e > 0.0f) ? 0.0f : cpow(b, e); }
 
 template <int S>
 __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMaterial& m, f3 w, const VSOut* t) {
     if constexpr (S == kFlat) {
-        f3 n = normalize(bary(w, t[0].normal, t[1].normal, t[2].normal));
+        f3 n = cnormalize(bary(w, t[0].normal, t[1].normal, t[2].normal));
         float intensity = sclamp(dot(neg(mk3(u.light_dir[0], u.light_dir[1], u.light_dir[2])), n), 0.0f, 1.0f);
         float c = fmul(1.0f, intensity);
         return mk4(c, c, c, c);
@@ -236,21 +242,21 @@ __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMat
         const float pi = 3.14159265358979323846f;
         float ndoth2 = fmul(ndoth, ndoth);
         float dp = fadd(fmul(ndoth2, fsub(r4, 1.0f)), 1.0f);
-        float ndf = fdiv(r4, fmul(fmul(pi, dp), dp));
+        float ndf = cdiv(r4, fmul(fmul(pi, dp), dp));
         float r = fadd(roughness, 1.0f);
-        float k = fdiv(fmul(r, r), 8.0f);
+        float k = cdiv(fmul(r, r), 8.0f);
         float nvk = fadd(fmul(ndotv, fsub(1.0f, k)), k);
         float nlk = fadd(fmul(ndotl, fsub(1.0f, k)), k);
-        float g = fmul(fdiv(ndotv, nvk), fdiv(ndotl, nlk));
+        float g = fmul(cdiv(ndotv, nvk), cdiv(ndotl, nlk));
         f3 f = fresnel_schlick(smax(dot(halfway, normal), 0.0f), f0);
         f3 numerator = mul(mul(f, ndf), g);
         float denom = fadd(fmul(fmul(4.0f, ndotv), ndotl), 0.0001f);
-        f3 specular = divs(numerator, denom);
+        f3 specular = cdivs(numerator, denom);
         f3 kd = mul(sub(one, f), one_minus_metallic);
-        f3 diffuse = mul(mul(kd, albedo), frcp(pi));
+        f3 diffuse = mul(mul(kd, albedo), crcp(pi));
         f3 ambient = mul(mul(mk3(0.03f, 0.03f, 0.03f), albedo), ao);
         f3 c = add(ambient, mul(mul(add(diffuse, specular), lc), ndotl));
-        c = div(c, add(c, one));
+        c = cdiv(c, add(c, one));
         const float inv_gamma = 1.0f / 2.2f;
         c = pow3(c, mk3(inv_gamma, inv_gamma, inv_gamma));
         return mk4(c.x, c.y, c.z, 1.0f);

@@ -66,3 +66,34 @@ def assert_parity(got, exp, what=""):
     assert d["depth_mismatch"] == 0, f"{what}: depth differs at {d['depth_mismatch']} pixels ({d})"
     assert d["color_max_lsb"] <= COLOR_TOLERANCE_LSB, f"{what}: colour differs by more than 1 LSB ({d})"
     return d
+
+
+def _const_tex(rgba, size=8):
+    return np.broadcast_to(np.array(rgba, np.uint8), (size, size, 4)).copy()
+
+
+# Lighting at its sharpest: specular exponent 50 * Ns of 0, 1, 1000 and 50,000 (a highlight a
+# few pixels wide), and PBR on a flat normal map with roughness 0, 1/255 (the distribution
+# term a spike that depends on n.h to the last bits) and 40/255, metallic 0 and 1.
+SHADING_EXTREMES = {
+    **{f"blinn_ns{ns:g}": (W.SHADER_BLINN_PHONG, dict(specular_exponent=ns)) for ns in (0.0, 0.02, 20.0, 1000.0)},
+    **{f"phong_ns{ns:g}": (W.SHADER_PHONG, dict(specular_exponent=ns, bump=(128, 128, 255, 255)))
+       for ns in (0.0, 20.0, 1000.0)},
+    **{f"pbr_r{r}_m{m}": (W.SHADER_PBR, dict(bump=(128, 128, 255, 255), roughness=(r, r, r, 255),
+                                             metallic=(m, m, m, 255), ao=(255, 255, 255, 255)))
+       for r in (0, 1, 40) for m in (0, 255)},
+}
+
+
+def shading_extreme_scene(name):
+    """A dense smooth sphere (192x96 segments, 320x240) lit for a highlight in view, with the
+    material of SHADING_EXTREMES[name]."""
+    kind, opts = SHADING_EXTREMES[name]
+    sc = W.sphere_scene(width=320, height=240, lon=192, lat=96, shader=kind, name=name)
+    ld = np.array([-0.3, -0.4, -1.0], np.float32)
+    sc.shader = W.Shader(kind, light_direction=tuple(map(float, ld / np.linalg.norm(ld))),
+                         light_color=sc.shader.light_color)
+    mat = sc.mesh.materials[0]
+    for k, v in opts.items():
+        setattr(mat, k, _const_tex(v) if isinstance(v, tuple) else v)
+    return sc

@@ -7,7 +7,7 @@ import pytest
 
 from axiomr_gb300 import api
 from axiomr_gb300 import workloads as W
-from helpers import GOLDEN, assert_parity, frame_diff, golden_names, load_golden
+from helpers import SHADING_EXTREMES, GOLDEN, assert_parity, frame_diff, golden_names, load_golden, shading_extreme_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -113,3 +113,15 @@ def test_gpu_camera_from_params_equals_explicit(ctx, port):
     a = api.render_scene(ctx, sc)
     b = api.render_scene(ctx, sc, view_proj=port.camera(sc.camera)[2])
     assert frame_diff(a, b)["depth_mismatch"] == 0 and np.array_equal(a[0], b[0])
+
+
+@pytest.mark.parametrize("name", sorted(SHADING_EXTREMES))
+def test_gpu_shading_extremes_match_oracle(ctx, port, name):
+    """Lighting terms at their sharpest (the colour path's divisions and powers are the
+    fast forms; normalisation stays correctly rounded): a dense smooth sphere with the
+    light placed for a highlight in view, against the oracle."""
+    sc = shading_extreme_scene(name)
+    vp = port.camera(sc.camera)[2]
+    exp = port.draw(sc, vp)
+    got = api.render_scene(ctx, sc, view_proj=vp)
+    assert_parity(got, exp, f"gpu vs oracle {name}")

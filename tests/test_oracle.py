@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from axiomr_gb300 import workloads as W
-from helpers import GOLDEN, assert_parity, golden_names, load_golden, same_bits
+from helpers import GOLDEN, SHADING_EXTREMES, assert_parity, golden_names, load_golden, same_bits, shading_extreme_scene
 
 X86 = platform.machine() in ("x86_64", "AMD64")
 
@@ -72,6 +72,14 @@ def test_port_equals_reference(ref, port, make):
     assert np.array_equal(r[2], p[2]), "camera matrices differ"
     assert_parity(p[:2], r[:2], sc.name)
     assert np.array_equal(p[0], r[0])
+
+
+@pytest.mark.parametrize("name", sorted(SHADING_EXTREMES))
+def test_port_equals_reference_shading_extremes(ref, port, name):
+    sc = shading_extreme_scene(name)
+    vp = port.camera(sc.camera)[2]
+    p, r = port.draw(sc, vp), ref.draw(sc, vp)
+    assert same_bits(p[1], r[1]) and np.array_equal(p[0], r[0])
 
 
 def test_port_equals_reference_stages_random(ref, port):
