@@ -223,6 +223,9 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->aux.stream, cudaStreamNonBlocking, prio_low);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->aux.join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->batch_side.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->batch_side.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->batch_side.join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, sizeof(DevCounters));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->batch_prof, sizeof(BatchProfile));
@@ -231,16 +234,11 @@ axr_status axr_context_create(int32_t device, axr_context** out) {
         axr_status st = cuda_fail(nullptr, e, "context setup");
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
         if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
-    for (int k = 0; k < axr_context::kCopyStreams; ++k) {
-        if (ctx->copy_stream[k]) {
-            cudaStreamSynchronize(ctx->copy_stream[k]);
-            cudaStreamDestroy(ctx->copy_stream[k]);
-        }
-        if (ctx->copy_join[k]) cudaEventDestroy(ctx->copy_join[k]);
-    }
-    if (ctx->copy_fork) cudaEventDestroy(ctx->copy_fork);
         if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
         if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
+        if (ctx->batch_side.stream) cudaStreamDestroy(ctx->batch_side.stream);
+        if (ctx->batch_side.fork) cudaEventDestroy(ctx->batch_side.fork);
+        if (ctx->batch_side.join) cudaEventDestroy(ctx->batch_side.join);
         dfree(ctx->counters);
         dfree(ctx->batch_prof);
         delete ctx;
@@ -281,6 +279,12 @@ void axr_context_destroy(axr_context* ctx) {
     if (ctx->copy_fork) cudaEventDestroy(ctx->copy_fork);
     if (ctx->aux.fork) cudaEventDestroy(ctx->aux.fork);
     if (ctx->aux.join) cudaEventDestroy(ctx->aux.join);
+    if (ctx->batch_side.stream) {
+        cudaStreamSynchronize(ctx->batch_side.stream);
+        cudaStreamDestroy(ctx->batch_side.stream);
+    }
+    if (ctx->batch_side.fork) cudaEventDestroy(ctx->batch_side.fork);
+    if (ctx->batch_side.join) cudaEventDestroy(ctx->batch_side.join);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }

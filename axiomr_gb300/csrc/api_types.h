@@ -65,12 +65,15 @@ struct axr_framebuffer {
 struct axr_batch {
     struct Launch {
         int shader;
+        int set;  // launch set: 0 on the context stream, 1 on the batch side stream
         axr::BatchParams params;
     };
     int device = 0;
     void* dev = nullptr;
     size_t bytes = 0;
     std::vector<Launch> launches;
+    int sets = 1;                               // launch sets (phased form of a large batch: 2)
+    axr::DevCounters* set_counters = nullptr;  // counters of launch set 1 (in `dev`)
     int form = 0;  // axr::kForm*
     uint32_t count = 0;
     uint64_t vertices = 0, faces = 0, pixels = 0, tiles = 0;
@@ -92,6 +95,7 @@ struct axr_context {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     axr::AuxStream aux{};  // side stream + fork/join events for the clipped-winner pass
+    axr::AuxStream batch_side{};  // second launch set of a split batch (normal priority)
     // read-back streams of axr_framebuffers_read_async (created on first use): copies of many
     // framebuffers are spread over them so that several copy engines run at once
     static constexpr int kCopyStreams = 4;

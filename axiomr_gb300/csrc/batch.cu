@@ -613,6 +613,19 @@ __global__ void __launch_bounds__(kBatchBlock) batch_clear_kernel(const __grid_c
     }
 }
 
+__global__ void merge_counters_kernel(DevCounters* dst, DevCounters* src) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint32_t err = src->error;
+    if (err) atomicOr(&dst->error, err);
+    src->error = 0u;
+    unsigned long long* d = &dst->stat_triangles;
+    unsigned long long* s = &src->stat_triangles;
+    for (int k = 0; k < 6; ++k) {  // stat_triangles .. stat_shaded
+        if (s[k]) atomicAdd(&d[k], s[k]);
+        s[k] = 0ull;
+    }
+}
+
 // Failure-path probe: CTA 0 waits at a grid barrier that CTA 1 never reaches, so the
 // bounded wait gives up after timeout_ns and sets kErrBarrier.
 __global__ void barrier_probe_kernel(DevCounters* c, unsigned long long timeout_ns) {
@@ -691,6 +704,11 @@ cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sm
         case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_merge_counters(DevCounters* dst, DevCounters* src, cudaStream_t stream) {
+    merge_counters_kernel<<<1, 32, 0, stream>>>(dst, src);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_barrier_probe(DevCounters* counters, unsigned long long timeout_ns, cudaStream_t stream) {

@@ -17,6 +17,10 @@ namespace axr {
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
                          cudaEvent_t* phase_events, uint64_t* launches);
 
+// Adds the statistics and error bits of `src` (a second launch set's counters) to `dst`
+// and zeroes them in `src` (one thread).
+cudaError_t launch_merge_counters(DevCounters* dst, DevCounters* src, cudaStream_t stream);
+
 // Failure-path probe of the grid barrier: one CTA waits at a barrier the other never
 // reaches; the bounded wait gives up after timeout_ns and sets the barrier error bit.
 cudaError_t launch_barrier_probe(DevCounters* counters, unsigned long long timeout_ns, cudaStream_t stream);

@@ -125,8 +125,16 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     }
     // shared large-triangle lists: a triangle that finds them full is rasterised by its own
     // thread instead, so the sizes trade memory for speed only
-    const uint32_t large_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(faces, 65536), 1u << 22);
-    const uint32_t item_cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(4 * faces, 1u << 20), 1u << 24);
+    const uint32_t large_cap_all = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(faces, 65536), 1u << 22);
+    const uint32_t item_cap_all = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(4 * faces, 1u << 20), 1u << 24);
+    // The phased form of a large batch runs as two launch sets of alternating draws, one on
+    // the context stream and one on a side stream, each with its own counters and
+    // large-triangle lists (the lists' capacity is shared out): one set's phases fill the
+    // other's tails and gaps, e.g. the issue-bound large-triangle phase beside the
+    // latency-bound tile pass.
+    const int nsets = (ctx->batch_form == kFormPhased && count >= (int32_t)kSplitMinDraws) ? 2 : 1;
+    const uint32_t large_cap = std::max<uint32_t>(65536, (large_cap_all + nsets - 1) / nsets);
+    const uint32_t item_cap = std::max<uint32_t>(1u << 20, (item_cap_all + nsets - 1) / nsets);
     // work units of every draw (the same counts as the loop below assigns)
     const int form = ctx->batch_form;
     const uint32_t tiles_per_warp = form == kFormPersistent ? kPersistentTilesPerWarp : kPhasedTilesPerWarp;
@@ -143,10 +151,12 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     }
     const size_t table_bytes = align256(sizeof(BatchDraw) * (size_t)std::max(count, 1));
     const size_t units_bytes = align256(sizeof(UnitRef) * std::max<size_t>(total_units, 1));
-    const size_t list_bytes = align256(sizeof(LargeTri) * (size_t)large_cap) +
-                              align256(sizeof(uint32_t) * (size_t)large_cap) +
-                              align256(sizeof(LargeItem) * (size_t)item_cap);
-    const size_t need = table_bytes + units_bytes + align256(cache_bytes) + list_bytes;
+    const size_t set_list_bytes = align256(sizeof(LargeTri) * (size_t)large_cap) +
+                                  align256(sizeof(uint32_t) * (size_t)large_cap) +
+                                  align256(sizeof(LargeItem) * (size_t)item_cap);
+    const size_t counter_bytes = align256(sizeof(DevCounters));
+    const size_t need = table_bytes + units_bytes + align256(cache_bytes) + set_list_bytes * nsets +
+                        counter_bytes * (nsets - 1);
     if (need > b->bytes) {
         if (ctx->capturing) return fail(ctx, AXR_E_CAPACITY, "a batch cannot be planned during graph capture");
         AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -159,10 +169,22 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     UnitRef* d_units = reinterpret_cast<UnitRef*>(base + table_bytes);
     unsigned char* cache = base + table_bytes + units_bytes;
     unsigned char* lists = cache + align256(cache_bytes);
-    LargeTri* d_large = reinterpret_cast<LargeTri*>(lists);
-    uint32_t* d_large_draw = reinterpret_cast<uint32_t*>(lists + align256(sizeof(LargeTri) * (size_t)large_cap));
-    LargeItem* d_items = reinterpret_cast<LargeItem*>(reinterpret_cast<unsigned char*>(d_large_draw) +
-                                                      align256(sizeof(uint32_t) * (size_t)large_cap));
+    LargeTri* d_large[2];
+    uint32_t* d_large_draw[2];
+    LargeItem* d_items[2];
+    DevCounters* d_counters[2] = {ctx->counters, nullptr};
+    for (int s = 0; s < nsets; ++s) {
+        unsigned char* l = lists + set_list_bytes * (size_t)s;
+        d_large[s] = reinterpret_cast<LargeTri*>(l);
+        d_large_draw[s] = reinterpret_cast<uint32_t*>(l + align256(sizeof(LargeTri) * (size_t)large_cap));
+        d_items[s] = reinterpret_cast<LargeItem*>(reinterpret_cast<unsigned char*>(d_large_draw[s]) +
+                                                  align256(sizeof(uint32_t) * (size_t)large_cap));
+    }
+    if (nsets > 1) {
+        d_counters[1] = reinterpret_cast<DevCounters*>(lists + set_list_bytes * (size_t)nsets);
+        // statistics and error bits start at zero; the merge after each launch zeroes them again
+        AXR_CUDA(ctx, cudaMemsetAsync(d_counters[1], 0, sizeof(DevCounters), ctx->stream));
+    }
 
     std::vector<BatchDraw> table((size_t)std::max(count, 1));
     std::vector<UnitRef> units;
@@ -170,8 +192,10 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     b->launches.clear();
     for (const auto& g : groups) {
         const size_t first = g.second.first, last = g.second.second, n = last - first;
-        std::vector<UnitRef> uv, uf, ut, uc;
+        std::vector<UnitRef> set_uv[2], set_uf[2], set_ut[2], set_uc[2];
         for (size_t k = 0; k < n; ++k) {
+            const int set = (int)(k % (size_t)nsets);
+            std::vector<UnitRef>&uv = set_uv[set], &uf = set_uf[set], &ut = set_ut[set], &uc = set_uc[set];
             const axr_draw_desc& d = draws[order[first + k]];
             const axr_mesh* m = d.mesh;
             const axr_framebuffer* fb = d.framebuffer;
@@ -191,8 +215,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             cache += align256(16 * (size_t)m->num_vertices * (size_t)vattr_float4s(d.shader.kind));
             float4* rec = reinterpret_cast<float4*>(cache);
             cache += align256(16 * (size_t)kRecFloat4 * m->num_drawn);
-            p.scratch = DevScratch{ctx->counters, d_large, d_items, vscreen, vattr, nullptr, nullptr,
-                                   large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw, rec};
+            p.scratch = DevScratch{d_counters[set], d_large[set], d_items[set], vscreen, vattr, nullptr, nullptr,
+                                   large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw[set], rec};
             p.small_max_pixels = ctx->tune_small[density_class(d)];
             p.draw = (uint32_t)k;
             bd.flags = (d.clear_flags & AXR_DRAW_CLEAR_COLOR ? kBatchClearColor : 0u) |
@@ -218,29 +242,33 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
                 for (uint32_t j = 0; j < nc; ++j) uc.push_back(UnitRef{(uint32_t)k, j});
             }
         }
-        const size_t unit_at = units.size();
-        units.insert(units.end(), uv.begin(), uv.end());
-        units.insert(units.end(), uf.begin(), uf.end());
-        units.insert(units.end(), ut.begin(), ut.end());
-        units.insert(units.end(), uc.begin(), uc.end());
-        axr_batch::Launch L{};
-        L.shader = g.first;
-        BatchParams& bp = L.params;
-        bp.draws = d_table + first;
-        bp.units = d_units + unit_at;
-        bp.counters = ctx->counters;
-        bp.large = d_large;
-        bp.items = d_items;
-        bp.large_draw = d_large_draw;
-        bp.count = (uint32_t)n;
-        bp.vert_units = (uint32_t)uv.size();
-        bp.face_units = (uint32_t)uf.size();
-        bp.tile_units = (uint32_t)ut.size();
-        bp.clear_units = (uint32_t)uc.size();
-        bp.large_cap = large_cap;
-        bp.item_cap = item_cap;
-        bp.tiles_per_warp = tiles_per_warp;
-        if (bp.vert_units + bp.face_units + bp.tile_units > 0) b->launches.push_back(L);
+        for (int set = 0; set < nsets; ++set) {
+            const std::vector<UnitRef>&uv = set_uv[set], &uf = set_uf[set], &ut = set_ut[set], &uc = set_uc[set];
+            const size_t unit_at = units.size();
+            units.insert(units.end(), uv.begin(), uv.end());
+            units.insert(units.end(), uf.begin(), uf.end());
+            units.insert(units.end(), ut.begin(), ut.end());
+            units.insert(units.end(), uc.begin(), uc.end());
+            axr_batch::Launch L{};
+            L.shader = g.first;
+            L.set = set;
+            BatchParams& bp = L.params;
+            bp.draws = d_table + first;  // unit references index the group's draws
+            bp.units = d_units + unit_at;
+            bp.counters = d_counters[set];
+            bp.large = d_large[set];
+            bp.items = d_items[set];
+            bp.large_draw = d_large_draw[set];
+            bp.count = (uint32_t)n;
+            bp.vert_units = (uint32_t)uv.size();
+            bp.face_units = (uint32_t)uf.size();
+            bp.tile_units = (uint32_t)ut.size();
+            bp.clear_units = (uint32_t)uc.size();
+            bp.large_cap = large_cap;
+            bp.item_cap = item_cap;
+            bp.tiles_per_warp = tiles_per_warp;
+            if (bp.vert_units + bp.face_units + bp.tile_units > 0) b->launches.push_back(L);
+        }
     }
     if (async) {
         // through pinned staging, so that the copies are queued without waiting for the work
@@ -270,6 +298,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             AXR_CUDA(ctx, cudaMemcpy(d_units, units.data(), sizeof(UnitRef) * units.size(), cudaMemcpyHostToDevice));
     }
     b->device = ctx->device;
+    b->sets = nsets;
+    b->set_counters = d_counters[1];
     b->form = form;
     b->count = (uint32_t)count;
     b->vertices = verts;
@@ -280,6 +310,15 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
 }
 
 axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
+    // a split batch: set 1 on the side stream, forked from and joined back into the context
+    // stream (a capture records the same fork and join); with phase timing on, the sets run
+    // in turn on the context stream so that each launch's phase events bracket its kernels
+    const bool split = b->sets > 1 && !ctx->profile;
+    cudaStream_t side = split ? ctx->batch_side.stream : ctx->stream;
+    if (split) {
+        AXR_CUDA(ctx, cudaEventRecord(ctx->batch_side.fork, ctx->stream));
+        AXR_CUDA(ctx, cudaStreamWaitEvent(side, ctx->batch_side.fork, 0));
+    }
     for (const axr_batch::Launch& L : b->launches) {
         BatchParams bp = L.params;
         bp.collect_stats = ctx->collect_stats;
@@ -294,7 +333,18 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
             ev = &ctx->batch_events[ctx->batch_events_used];
             ctx->batch_events_used += 6;
         }
-        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, ctx->stream, ev, &ctx->launches));
+        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, L.set ? side : ctx->stream, ev,
+                                   &ctx->launches));
+    }
+    if (b->sets > 1) {
+        // set 1's statistics and error bits into the context's counters, which axr_sync and
+        // axr_stats_read report
+        AXR_CUDA(ctx, launch_merge_counters(ctx->counters, b->set_counters, side));
+        ctx->launches += 1;
+    }
+    if (split) {
+        AXR_CUDA(ctx, cudaEventRecord(ctx->batch_side.join, side));
+        AXR_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->batch_side.join, 0));
     }
     return AXR_OK;
 }

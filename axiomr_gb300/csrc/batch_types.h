@@ -88,6 +88,7 @@ constexpr int kFormPersistent = 0;
 constexpr int kFormPhased = 1;
 constexpr uint32_t kPersistentTilesPerWarp = 8;
 constexpr uint32_t kPhasedTilesPerWarp = 4;
+constexpr uint32_t kSplitMinDraws = 128;  // phased batches of this many draws run as two launch sets
 static_assert(kUnitWarps * kPhasedTilesPerWarp <= 32, "a phased tile unit is described by 32-bit tile masks");
 
 }  // namespace axr

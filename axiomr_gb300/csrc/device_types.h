@@ -13,6 +13,7 @@
 //   visibility keys, all-ones between draws), tile_flag[TX*TY] uint32 (16x16 tile holds a
 //   key; set by the rasterisers, cleared by the key scan).
 #pragma once
+#include <stddef.h>
 #include <stdint.h>
 #include <vector_types.h>
 
@@ -115,6 +116,8 @@ struct DevCounters {
     unsigned long long stat_tested;      // (triangle, pixel) coverage tests evaluated
     unsigned long long stat_shaded;      // winning fragments shaded
 };
+static_assert(offsetof(DevCounters, stat_shaded) == offsetof(DevCounters, stat_triangles) + 5 * 8,
+              "the six statistics are consecutive (merged as an array)");
 
 constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
 constexpr unsigned kBatchCountersReset = 7 * sizeof(uint32_t);  // + the grid-barrier words

@@ -210,12 +210,13 @@ def measured_peaks():
 
 
 def profiled_traffic(kernel: str, workload: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    """DRAM bytes of `kernel` from the committed ncu summary, if any: per launch, or per step
+    where a step launches it more than once (the batched form's two launch sets)."""
     f = ROOT / "profiles" / f"{kernel}_{workload}.txt"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith("dram_bytes_per_launch:") or line.startswith("dram_bytes_per_step:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -763,12 +764,15 @@ def run_batch(args, dist: Dist):
     # per-phase device time of one batch (eager launches with profiling on)
     ctx.profile(True)
     ctx.profile()
-    for _ in range(3):
+    n_prof = 3
+    for _ in range(n_prof):
         batch.launch()
     pr = ctx.profile()
     ctx.profile(False)
-    nl = max(1, pr["batch_launches"])
-    phase_ms = {k: pr[f"batch_{k}_ms"] / nl for k in ("clear", "vertex", "face", "large", "tile")}
+    # per step: the sum over the step's launches of each phase (a split batch launches every
+    # phase once per launch set; with timing on the sets run in turn)
+    phase_ms = {k: pr[f"batch_{k}_ms"] / n_prof for k in ("clear", "vertex", "face", "large", "tile")}
+    launches_per_step = max(1, pr["batch_launches"] // n_prof)
 
     fp32_tflops = ctx.fp32_peak_tflops()
     hbm_peak, peak_kind = measured_peaks()
@@ -794,7 +798,10 @@ def run_batch(args, dist: Dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
         "config": {"workload": f"batch: {desc}",
-                   "form": ("batched, phased: a clear kernel and four phase launches per step over the work "
+                   "form": ("batched, phased: a clear kernel and four phase launches over the work units of "
+                            "all draws, as two launch sets of alternating draws on two streams"
+                            if info["form"] == 1 and info["launches"] > 1 else
+                            "batched, phased: a clear kernel and four phase launches per step over the work "
                             "units of all draws" if info["form"] == 1 else
                             "batched, persistent: one cooperative launch per step (clears fused into the tile pass)")
                    + ", replayed from a CUDA graph",
@@ -834,7 +841,10 @@ def run_batch(args, dist: Dist):
         "roofline": {"bound": "hbm", "kernel": kernel_of[dom], "phase": dom, "achieved": round(dom_achieved, 1),
                      "peak": hbm_peak, "peak_source": peak_kind, "unit": "GB/s",
                      "frac": round(dom_achieved / hbm_peak, 4), "traffic": profiled_traffic(kernel_of[dom], "batch"),
-                     "algorithmic_bytes": pb[dom], "launch_us": round(phase_ms[dom] * 1e3, 2),
+                     "algorithmic_bytes": pb[dom], "kernel_us_per_step": round(phase_ms[dom] * 1e3, 2),
+                     "launches_per_step": launches_per_step,
+                     "per": "step: algorithmic bytes, traffic and kernel time summed over the step's launches "
+                            "of the kernel (one per launch set)",
                      "phase_us": {k: round(v * 1e3, 2) for k, v in phase_ms.items()}},
         "frame_roofline": {"bound": "hbm" if achieved / hbm_peak >= alu_tflops / fp32_tflops else "alu",
                            "hbm": {"achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",

@@ -320,3 +320,44 @@ def test_grid_barrier_timeout_reports_and_context_survives(ctx):
         ctx.batch_form = saved
     for k in range(len(scenes)):
         assert_same(frames[api.BATCH_PERSISTENT][k], frames[api.BATCH_PHASED][k], f"draw {k} after the timeout")
+
+
+def test_split_phased_batch_equals_unsplit(ctx):
+    """A phased batch of 128+ draws runs as two launch sets (context stream and a side
+    stream, own counters and lists): its frames and statistics equal those of the
+    persistent form (one launch set) on the same draws, eagerly and replayed from a graph."""
+    scenes = W.batch_scenes(count=130, seed=29, tex_size=64, resolution_scale=0.1)
+    draws = api.batch_draws(ctx, scenes)
+    saved = ctx.batch_form
+    frames, stats = {}, {}
+    try:
+        for form in (api.BATCH_PERSISTENT, api.BATCH_PHASED):
+            ctx.batch_form = form
+            batch = api.Batch(ctx, draws)
+            for d in draws:
+                d.framebuffer.clearColor(7, 7, 7, 7)
+            ctx.stats(True)
+            ctx.stats()  # reset
+            batch.launch()
+            stats[form] = ctx.stats()
+            ctx.stats(False)
+            frames[form] = [d.framebuffer.read() for d in draws]
+            if form == api.BATCH_PHASED:
+                assert batch.info()["launches"] == 2  # one shader kind, two launch sets
+                for d in draws:
+                    d.framebuffer.clearColor(9, 9, 9, 9)
+                    d.framebuffer.clearDepth(-1.0)
+                g = api.Graph(ctx).begin()
+                batch.launch()
+                g.end()
+                g.launch()
+                ctx.sync()
+                for k, d in enumerate(draws):
+                    assert_same(d.framebuffer.read(), frames[form][k], f"graph replay of the split batch, draw {k}")
+                g.close()
+            batch.close()
+    finally:
+        ctx.batch_form = saved
+    for k in range(len(draws)):
+        assert_same(frames[api.BATCH_PHASED][k], frames[api.BATCH_PERSISTENT][k], f"split vs persistent, draw {k}")
+    assert stats[api.BATCH_PHASED] == stats[api.BATCH_PERSISTENT] and stats[api.BATCH_PHASED]["shaded"] > 0
