@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -50,6 +51,18 @@ axr_status cuda_fail(axr_context* ctx, cudaError_t e, const char* what) {
 
 void dfree(void* p) {
     if (p) cudaFree(p);
+}
+
+void mesh_sync_bounds(const axr_mesh* m) {
+    if (!m || !m->bounds_pending) return;
+    if (cudaEventSynchronize(m->bounds_ready) != cudaSuccess) return;  // keep the previous bounds
+    const MeshBounds& b = *m->bounds_host;
+    for (int k = 0; k < 3; ++k)
+        m->bound_center[k] = 0.5f * (mesh_bounds_float(b.lo[k]) + mesh_bounds_float(b.hi[k]));
+    double r2;
+    std::memcpy(&r2, &b.r2, sizeof(r2));
+    m->bound_radius = m->num_vertices ? (float)std::sqrt(r2) * 1.0001f : 0.f;
+    m->bounds_pending = false;
 }
 
 }  // namespace axr_internal
@@ -172,7 +185,12 @@ axr_status upload_mesh_arrays(axr_context* ctx, axr_mesh* m, const axr_mesh_desc
 void free_mesh(axr_mesh* m) {
     if (!m) return;
     dfree(m->pos); dfree(m->nrm); dfree(m->tan); dfree(m->bit); dfree(m->uv); dfree(m->idx);
-    dfree(m->groups); dfree(m->materials); dfree(m->staging);
+    dfree(m->groups); dfree(m->materials); dfree(m->staging); dfree(m->bounds_dev);
+    if (m->bounds_ready) {
+        cudaEventSynchronize(m->bounds_ready);
+        cudaEventDestroy(m->bounds_ready);
+    }
+    if (m->bounds_host) cudaFreeHost(m->bounds_host);
     delete m;
 }
 
@@ -460,6 +478,10 @@ axr_status axr_mesh_create(axr_context* ctx, const axr_mesh_desc* d, axr_mesh** 
     return AXR_OK;
 }
 
+// Above this many vertices axr_mesh_update computes the bounds on the device (five small
+// stream operations cost about as much as a host pass over 8k vertices).
+constexpr uint32_t kHostBoundsMaxVertices = 8192;
+
 axr_status axr_mesh_update(axr_context* ctx, axr_mesh* m, const axr_mesh_desc* d) {
     if (!ctx || !m || !d) return fail(ctx, AXR_E_INVALID, "NULL argument");
     if (d->num_vertices != m->num_vertices || d->num_faces != m->num_faces)
@@ -471,8 +493,28 @@ axr_status axr_mesh_update(axr_context* ctx, axr_mesh* m, const axr_mesh_desc* d
     if (d->num_faces && !d->indices) return fail(ctx, AXR_E_INVALID, "mesh update needs indices");
     std::lock_guard<std::mutex> lk(ctx->mu);
     DeviceGuard g(ctx->device);
-    mesh_bounds(d->positions, d->num_vertices, m->bound_center, &m->bound_radius);
-    return upload_mesh_arrays(ctx, m, d);
+    axr_status st = upload_mesh_arrays(ctx, m, d);
+    if (st != AXR_OK) return st;
+    // the bounding sphere of the new positions: a host pass for a small mesh (a few us);
+    // for a large one on the device behind the upload (a host pass over a million vertices
+    // takes milliseconds), which batch planning waits for if it must
+    if (m->num_vertices <= kHostBoundsMaxVertices) {
+        mesh_bounds(d->positions, d->num_vertices, m->bound_center, &m->bound_radius);
+        m->bounds_pending = false;
+        return AXR_OK;
+    }
+    if (!m->bounds_dev) {
+        AXR_CUDA(ctx, cudaMalloc(&m->bounds_dev, sizeof(MeshBounds)));
+        AXR_CUDA(ctx, cudaMallocHost(&m->bounds_host, sizeof(MeshBounds)));
+        AXR_CUDA(ctx, cudaEventCreateWithFlags(&m->bounds_ready, cudaEventDisableTiming));
+    }
+    AXR_CUDA(ctx, launch_mesh_bounds(m->pos, m->num_vertices, m->bounds_dev, ctx->stream));
+    AXR_CUDA(ctx, cudaMemcpyAsync(m->bounds_host, m->bounds_dev, sizeof(MeshBounds), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    AXR_CUDA(ctx, cudaEventRecord(m->bounds_ready, ctx->stream));
+    m->bounds_pending = true;
+    ctx->launches += m->num_vertices ? 2 : 0;
+    return AXR_OK;
 }
 
 void axr_mesh_destroy(axr_context* ctx, axr_mesh* m) {

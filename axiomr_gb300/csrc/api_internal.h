@@ -28,6 +28,8 @@ void dfree(void* p);
 void encode_framebuffer_maps(axr_framebuffer* fb);
 // Bounding sphere (box centre, largest distance) of n float3 positions.
 void mesh_bounds(const float* pos, uint32_t n, float center[3], float* radius);
+// Waits for and takes the device-computed bounds of the last axr_mesh_update, if any.
+void mesh_sync_bounds(const axr_mesh* m);
 // Release a batch's device memory (the caller synchronises first).
 void free_batch(axr_batch* b);
 // Release a batch's pinned staging and its events (the caller synchronises first).

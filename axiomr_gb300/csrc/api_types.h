@@ -43,8 +43,15 @@ struct axr_mesh {
     float* staging = nullptr;  // packed float3 upload area for updates
     uint32_t num_vertices = 0, num_faces = 0, num_groups = 0, num_materials = 0, num_drawn = 0;
     int device = 0;
-    float bound_center[3] = {0.f, 0.f, 0.f};  // bounding sphere of the positions (batch planning)
-    float bound_radius = 0.f;
+    // bounding sphere of the positions (batch planning): from the host arrays at creation;
+    // after axr_mesh_update computed on the device on the update's stream and copied into
+    // bounds_host behind bounds_ready (read through mesh_sync_bounds)
+    mutable float bound_center[3] = {0.f, 0.f, 0.f};
+    mutable float bound_radius = 0.f;
+    mutable bool bounds_pending = false;
+    axr::MeshBounds* bounds_dev = nullptr;
+    axr::MeshBounds* bounds_host = nullptr;  // pinned
+    cudaEvent_t bounds_ready = nullptr;
 };
 
 struct axr_framebuffer {

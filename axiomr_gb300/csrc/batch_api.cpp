@@ -49,6 +49,7 @@ int density_class(const axr_draw_desc& d) {
     const axr_mesh* m = d.mesh;
     const axr_framebuffer* fb = d.framebuffer;
     if (!m || !fb || m->num_drawn == 0) return 0;
+    mesh_sync_bounds(m);
     const float* M = d.model;
     const float* c = m->bound_center;
     double wc[3];

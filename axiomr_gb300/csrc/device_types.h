@@ -98,6 +98,14 @@ struct LargeItem {
 constexpr uint32_t kNoItem = 0xFFFFFFFFu;
 constexpr uint32_t kItemsPerGrab = 4;  // tiles a warp takes per atomic
 
+// Bounding box and squared bounding-sphere radius of a mesh's positions, computed on the
+// device after an update: lo/hi as order-preserving integers (see kernels.cu), r2 the
+// largest squared distance (double) from the box centre.
+struct MeshBounds {
+    uint32_t lo[3], hi[3];
+    unsigned long long r2;  // bits of a non-negative double
+};
+
 // Work counters of one draw: the first kCountersReset bytes are zeroed (a memset on
 // the stream) before every draw.
 struct DevCounters {

@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstring>
 
 #include "draw_body.cuh"
 #include "kernels.h"
@@ -366,6 +367,76 @@ cudaError_t launch_clear(uint32_t* color, float* depth, size_t pixels, uint32_t 
 cudaError_t launch_fill_u64(unsigned long long* dst, size_t n, unsigned long long v, cudaStream_t stream) {
     fill_u64_kernel<<<grid_for(n, 256, 4096), 256, 0, stream>>>(dst, n, v);
     return cudaGetLastError();
+}
+
+// ---- mesh bounds after an update (batch planning's density classes)
+__device__ __forceinline__ uint32_t float_ord(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_float(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
+}
+
+__global__ void mesh_box_kernel(const float4* __restrict__ pos, uint32_t n, MeshBounds* out) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = __ldg(pos + i);
+        const float v[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], v[k]);
+            hi[k] = fmaxf(hi[k], v[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&out->lo[k], float_ord(lo[k]));
+            atomicMax(&out->hi[k], float_ord(hi[k]));
+        }
+    }
+}
+
+__global__ void mesh_radius_kernel(const float4* __restrict__ pos, uint32_t n, MeshBounds* out) {
+    float c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[k] = __fmul_rn(0.5f, __fadd_rn(ord_float(out->lo[k]), ord_float(out->hi[k])));
+    double r2 = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = __ldg(pos + i);
+        const float v[3] = {p.x, p.y, p.z};
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double t = __dsub_rn((double)v[k], (double)c[k]);
+            s = __dadd_rn(s, __dmul_rn(t, t));
+        }
+        r2 = fmax(r2, s);
+    }
+    for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xFFFFFFFFu, r2, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&out->r2, (unsigned long long)__double_as_longlong(r2));
+}
+
+cudaError_t launch_mesh_bounds(const float4* pos, uint32_t n, MeshBounds* out, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(out->lo, 0xFF, sizeof(out->lo), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(out->hi, 0, sizeof(out->hi) + sizeof(out->r2), stream);
+    if (e != cudaSuccess || n == 0) return e;
+    const unsigned g = grid_for(n, 256, 1024);
+    mesh_box_kernel<<<g, 256, 0, stream>>>(pos, n, out);
+    mesh_radius_kernel<<<g, 256, 0, stream>>>(pos, n, out);
+    return cudaGetLastError();
+}
+
+float mesh_bounds_float(uint32_t o) {
+    const uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+    float f;
+    std::memcpy(&f, &u, sizeof(f));
+    return f;
 }
 
 cudaError_t launch_pack3(const float* src, float4* dst, uint32_t n, cudaStream_t stream) {

@@ -34,6 +34,11 @@ cudaError_t launch_clear(uint32_t* color, float* depth, size_t pixels, uint32_t 
 cudaError_t launch_fill_u64(unsigned long long* dst, size_t n, unsigned long long v, cudaStream_t stream);
 // float3 (packed) -> float4 (x, y, z, 0)
 cudaError_t launch_pack3(const float* src, float4* dst, uint32_t n, cudaStream_t stream);
+// Bounds of pos[0, n) into *out (device); the box centre and squared radius follow the
+// host's mesh_bounds operation for operation.
+cudaError_t launch_mesh_bounds(const float4* pos, uint32_t n, MeshBounds* out, cudaStream_t stream);
+// The float an order-preserving integer of launch_mesh_bounds stands for.
+float mesh_bounds_float(uint32_t ord);
 // RGBA8 bytes of a uint32 array (no conversion needed; provided for symmetry)
 
 // Stage dump for parity tests: every triangle that survives clip + cull, unordered, as

@@ -361,3 +361,34 @@ def test_split_phased_batch_equals_unsplit(ctx):
     for k in range(len(draws)):
         assert_same(frames[api.BATCH_PHASED][k], frames[api.BATCH_PERSISTENT][k], f"split vs persistent, draw {k}")
     assert stats[api.BATCH_PHASED] == stats[api.BATCH_PERSISTENT] and stats[api.BATCH_PHASED]["shaded"] > 0
+
+
+def test_mesh_update_refreshes_bounds_for_planning(ctx):
+    """axr_mesh_update of a mesh above 8,192 vertices computes the new positions' bounding
+    sphere on the device (no host pass over the arrays): a draw of the updated mesh falls in the same density class as
+    one of a mesh created from the same arrays, over model scales that cross every class
+    boundary; the frames of the two agree exactly."""
+    a = W.sphere_scene(width=96, height=96, lon=128, lat=64).mesh  # 8,385 vertices: the device path
+    b = W.heightfield_scene(n=100, width=96, height=96, tex_size=16).mesh
+    n = a.positions.shape[0]
+    pos = (b.positions[:n] * np.float32(2.5) + np.float32([0.3, -0.2, 0.1])).astype(np.float32)
+    mesh_a = api.Mesh(ctx, a.positions, a.uvs, a.normals, a.indices)
+    mesh_a.update(pos, a.uvs, a.normals, a.indices)
+    mesh_b = api.Mesh(ctx, pos, a.uvs, a.normals, a.indices)
+    fb_a, fb_b = api.Framebuffer(ctx, 96, 96), api.Framebuffer(ctx, 96, 96)
+    fb_big = api.Framebuffer(ctx, 2048, 2048)  # the classes need large screen areas per triangle
+    cam = api.Camera((0.0, 0.0, 6.0), (0.0, 0.0, 0.0), 60.0, 1.0)
+    seen = set()
+    for s in np.geomspace(0.02, 5.0, 40):
+        model = np.diag([s, s, s, 1.0]).astype(np.float32).reshape(16)
+        da = api.Draw(mesh_a, fb_big, cam, api.BlinnPhongShader(), model)
+        db = api.Draw(mesh_b, fb_big, cam, api.BlinnPhongShader(), model)
+        ca, cb = api.density_class(da), api.density_class(db)
+        assert ca == cb, (s, ca, cb)
+        seen.add(ca)
+    assert len(seen) >= 4
+    model = np.diag([0.3, 0.3, 0.3, 1.0]).astype(np.float32).reshape(16)
+    draws = [api.Draw(mesh_a, fb_a, cam, api.BlinnPhongShader(), model, (0, 0, 0, 255), float("inf")),
+             api.Draw(mesh_b, fb_b, cam, api.BlinnPhongShader(), model, (0, 0, 0, 255), float("inf"))]
+    api.draw_batch(ctx, draws)
+    assert_same(fb_a.read(), fb_b.read(), "updated vs created mesh")
