@@ -54,7 +54,10 @@ void dfree(void* p) {
 }
 
 void mesh_sync_bounds(const axr_mesh* m) {
-    if (!m || !m->bounds_pending) return;
+    static std::mutex mu;  // planners on several threads may share a mesh
+    if (!m) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!m->bounds_pending) return;
     if (cudaEventSynchronize(m->bounds_ready) != cudaSuccess) return;  // keep the previous bounds
     const MeshBounds& b = *m->bounds_host;
     for (int k = 0; k < 3; ++k)

@@ -173,7 +173,10 @@ axr_status axr_mesh_counts(const axr_mesh* mesh, uint32_t* vertices, uint32_t* f
 axr_status axr_mesh_create(axr_context* ctx, const axr_mesh_desc* desc, axr_mesh** out);
 /* Re-upload vertex attributes and indices of an existing mesh with the same counts,
  * asynchronously on the context stream (host buffers must stay valid until then;
- * pinned memory from axr_host_alloc makes the copies truly asynchronous). */
+ * pinned memory from axr_host_alloc makes the copies truly asynchronous). The mesh's
+ * bounding sphere, used to plan batches, is recomputed from the new positions (on the
+ * device for meshes above 8,192 vertices). Do not update a mesh while another context
+ * plans or draws with it. */
 axr_status axr_mesh_update(axr_context* ctx, axr_mesh* mesh, const axr_mesh_desc* desc);
 void axr_mesh_destroy(axr_context* ctx, axr_mesh* mesh);
 
