@@ -347,8 +347,11 @@ void axr_batch_destroy(axr_context* ctx, axr_batch* batch);
 
 /* Launch forms (the autotuner picks one per batch; batches planned afterwards use it):
  * PERSISTENT: one cooperative launch per shader kind, its four phases (vertices, faces,
- * large-triangle tiles, tile pass) behind grid barriers; PHASED: four launches per shader
- * kind, one per phase, each over the work units of every draw. */
+ * large-triangle tiles, tile pass) behind grid barriers; PHASED: a clear kernel and four
+ * launches per shader kind, one per phase, each over the work units of every draw. A
+ * phased batch of 128 or more draws runs each shader kind as two launch sets of
+ * alternating draws, the second on a side stream of the context (forked from and joined
+ * back into its stream, also inside a graph capture), so that the sets' phases overlap. */
 #define AXR_BATCH_PERSISTENT 0
 #define AXR_BATCH_PHASED 1
 axr_status axr_batch_set_form(axr_context* ctx, int32_t form);
@@ -356,7 +359,8 @@ int32_t axr_batch_get_form(const axr_context* ctx);
 
 typedef struct axr_batch_info {
     uint32_t draws;
-    uint32_t launches;        /* shader-kind groups (each one launch set) per axr_batch_launch */
+    uint32_t launches;        /* launch sets per axr_batch_launch: one per shader kind, two for a
+                               * phased batch of 128+ draws */
     int32_t form;             /* AXR_BATCH_* the batch was planned for */
     uint32_t pad_;
     uint64_t vertices;        /* vertices of all draws */
