@@ -200,6 +200,25 @@ __device__ __forceinline__ void vertex_one(const DrawParams& p, uint32_t i) {
     pack_vsout<S>(vertex_shader<S>(p.u, v), &p.scratch.vattr[(size_t)VAttr<S>::n * i]);
 }
 
+// A face whose vertices straddle the clip volume: the clipper's output triangles, each
+// emitted with its clip index in the tag and its tile marked here.
+__device__ __noinline__ void geometry_clipped(const DrawParams& p, uint32_t o, const uint3 f, uint32_t material,
+                                              GeomStats& st) {
+    CVClip a[kMaxClipVerts], b[kMaxClipVerts];
+    a[0].clip = load_clip(p.mesh, p.u.mvp, f.x);
+    a[1].clip = load_clip(p.mesh, p.u.mvp, f.y);
+    a[2].clip = load_clip(p.mesh, p.u.mvp, f.z);
+    CVClip* out;
+    const int n = clip_triangle<0>(a, b, &out);
+    for (int j = 0; 3 * j + 2 < n; ++j) {
+        Screen s;
+        screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width, p.target.height, s);
+        uint32_t tile = kNoTile;
+        emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile, f, material);
+        if (tile != kNoTile) mark_tile(p.target, tile);
+    }
+}
+
 // Face at draw-order position o (< num_drawn): clip classification, cull, setup and
 // raster or queueing (src/tiled_pipeline.cpp:195-240, 436-487).
 // kCoherent: the vertex cache was written earlier in the same launch (plain loads).
@@ -228,21 +247,65 @@ __device__ __forceinline__ void geometry_one(const DrawParams& p, uint32_t o, Ge
         screen_bbox(s);
         emit_triangle(p, s, o << 4, st, &single_tile, f, fr.material);
     } else if (cls < 0) {
-        CVClip a[kMaxClipVerts], b[kMaxClipVerts];
-        a[0].clip = load_clip(p.mesh, p.u.mvp, f.x);
-        a[1].clip = load_clip(p.mesh, p.u.mvp, f.y);
-        a[2].clip = load_clip(p.mesh, p.u.mvp, f.z);
-        CVClip* out;
-        const int n = clip_triangle<0>(a, b, &out);
-        for (int j = 0; 3 * j + 2 < n; ++j) {
-            Screen s;
-            screen_setup(out[3 * j].clip, out[3 * j + 1].clip, out[3 * j + 2].clip, p.target.width,
-                         p.target.height, s);
-            uint32_t tile = kNoTile;
-            emit_triangle(p, s, (o << 4) | 8u | (uint32_t)j, st, &tile, f, fr.material);
-            if (tile != kNoTile) mark_tile(p.target, tile);
-        }
+        geometry_clipped(p, o, f, fr.material, st);
     }
+}
+
+// A front-facing face inside the clip volume, queued by geometry_front for the setup and
+// raster pass of the compacted face phase.
+struct FaceJob {
+    float x[3], y[3], z[3];
+    uint32_t o, material;
+    uint32_t f[3];
+};
+
+// The first half of geometry_one for the compacted face phase: the checks, the vertex-cache
+// gathers, clip classification and the back-face test. A face that straddles the clip
+// volume is finished here; one inside it that faces the camera is returned in *job (true)
+// for emit_triangle in a second pass, where every lane of a warp has such a face.
+template <bool kCoherent>
+__device__ __forceinline__ bool geometry_front(const DrawParams& p, uint32_t o, GeomStats& st, FaceJob& job) {
+    if (o > kMaxOrdinal) {
+        atomicOr(&p.scratch.counters->error, kErrOrdinal);
+        return false;
+    }
+    const FaceRef fr = face_of(p.mesh, o);
+    const uint3 f = load_face(p.mesh, fr.face);
+    const uint32_t nv = p.mesh.num_vertices;
+    if (f.x >= nv || f.y >= nv || f.z >= nv) {
+        atomicOr(&p.scratch.counters->error, kErrIndex);
+        return false;
+    }
+    const float4* vs = p.scratch.vscreen;
+    const float4 g0 = ld_cached<kCoherent>(&vs[f.x]), g1 = ld_cached<kCoherent>(&vs[f.y]),
+                 g2 = ld_cached<kCoherent>(&vs[f.z]);
+    const int cls = classify_masks(__float_as_uint(g0.w), __float_as_uint(g1.w), __float_as_uint(g2.w));
+    if (cls == 3) {
+        Screen s;
+        s.x[0] = g0.x; s.y[0] = g0.y; s.z[0] = g0.z;
+        s.x[1] = g1.x; s.y[1] = g1.y; s.z[1] = g1.z;
+        s.x[2] = g2.x; s.y[2] = g2.y; s.z[2] = g2.z;
+        if (is_backface(s)) return false;
+        job = FaceJob{{s.x[0], s.x[1], s.x[2]}, {s.y[0], s.y[1], s.y[2]}, {s.z[0], s.z[1], s.z[2]},
+                      o, fr.material, {f.x, f.y, f.z}};
+        return true;
+    }
+    if (cls < 0) geometry_clipped(p, o, f, fr.material, st);
+    return false;
+}
+
+// The second half: setup and raster (or queueing) of a queued face, as geometry_one does.
+__device__ __forceinline__ void geometry_job(const DrawParams& p, const FaceJob& j, GeomStats& st,
+                                             uint32_t& single_tile) {
+    Screen s;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        s.x[k] = j.x[k];
+        s.y[k] = j.y[k];
+        s.z[k] = j.z[k];
+    }
+    screen_bbox(s);
+    emit_triangle(p, s, j.o << 4, st, &single_tile, make_uint3(j.f[0], j.f[1], j.f[2]), j.material);
 }
 
 // Warp-wide end of the geometry step: one mark per distinct single tile in the warp, and
