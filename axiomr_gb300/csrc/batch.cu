@@ -346,29 +346,6 @@ __device__ __forceinline__ void face_unit(const DrawParams& p, const UnitInfo& u
     geometry_warp_tail(p.target, c, stats, st, single_tile);
 }
 
-// The phased form's face unit in two passes: geometry_front per face (checks, gathers, clip
-// classification, back-face test), the front-facing faces compacted into `jobs` by warp
-// ballots, then geometry_job on them with every lane busy (about half the faces of a mesh
-// face away; without the compaction their lanes idle through their neighbours' setup and
-// raster loops).
-__device__ __forceinline__ void face_unit_compact(const DrawParams& p, const UnitInfo& ui, DevCounters* c, bool stats,
-                                                  FaceJob* jobs, uint32_t* count) {
-    GeomStats st = {0, 0, 0, 0};
-    uint32_t single_tile = kNoTile;
-    const uint32_t o = ui.local * kFaceUnit + threadIdx.x;
-    FaceJob job;
-    const bool queued = o < p.mesh.num_drawn && geometry_front<false>(p, o, st, job);
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, queued);
-    const int lane = threadIdx.x & 31;
-    uint32_t base = 0;
-    if (lane == 0 && m) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (queued) jobs[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = job;
-    __syncthreads();
-    if (threadIdx.x < *count) geometry_job(p, jobs[threadIdx.x], st, single_tile);
-    geometry_warp_tail(p.target, c, stats, st, single_tile);
-}
-
 // Large-triangle tile items of all draws, strided over every warp of the grid (items are
 // alike, 256 pixels each, so a static split balances without a shared counter).
 __device__ __forceinline__ void large_items(const BatchParams& bp, bool stats) {
@@ -511,7 +488,8 @@ __global__ void __launch_bounds__(kBatchBlock, 5) batch_face_kernel(const __grid
     if (threadIdx.x == 0) s_count = 0u;
     stage_unit(bp, bp.vert_units + blockIdx.x, &s_p, &s_u);
     __syncthreads();
-    face_unit_compact(s_p, s_u, bp.counters, bp.collect_stats != 0, s_jobs, &s_count);
+    geometry_compacted(s_p, s_u.local * kFaceUnit + threadIdx.x, bp.counters, bp.collect_stats != 0, s_jobs,
+                       &s_count);
 }
 
 __global__ void __launch_bounds__(kBatchBlock) batch_large_kernel(const __grid_constant__ BatchParams bp) {

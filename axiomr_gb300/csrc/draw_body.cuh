@@ -327,6 +327,28 @@ __device__ __forceinline__ void geometry_warp_tail(const DevTarget& t, DevCounte
     }
 }
 
+// One CTA's faces in two passes (every thread calls it with its face o; *count is zero on
+// entry; `jobs` holds one entry per thread): geometry_front per face, the front-facing
+// faces compacted into `jobs` by warp ballots, then geometry_job on them with every lane
+// busy. About half the faces of a closed mesh face away; without the compaction their
+// lanes idle through their neighbours' setup and raster loops.
+__device__ __forceinline__ void geometry_compacted(const DrawParams& p, uint32_t o, DevCounters* c, bool stats,
+                                                   FaceJob* jobs, uint32_t* count) {
+    GeomStats st = {0, 0, 0, 0};
+    uint32_t single_tile = kNoTile;
+    FaceJob job;
+    const bool queued = o < p.mesh.num_drawn && geometry_front<false>(p, o, st, job);
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, queued);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (queued) jobs[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = job;
+    __syncthreads();
+    if (threadIdx.x < *count) geometry_job(p, jobs[threadIdx.x], st, single_tile);
+    geometry_warp_tail(p.target, c, stats, st, single_tile);
+}
+
 // Whether no pixel of 16x16 tile (tx, ty) inside the triangle's box can test covered.
 // Each edge function is linear, so over the tile's pixel centres it peaks at a corner of
 // their rectangle. eval_pixel's float evaluation of an edge at a centre is within a few
