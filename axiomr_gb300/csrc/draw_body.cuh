@@ -328,10 +328,13 @@ __device__ __forceinline__ void geometry_warp_tail(const DevTarget& t, DevCounte
 }
 
 // One CTA's faces in two passes (every thread calls it with its face o; *count is zero on
-// entry; `jobs` holds one entry per thread): geometry_front per face, the front-facing
-// faces compacted into `jobs` by warp ballots, then geometry_job on them with every lane
-// busy. About half the faces of a closed mesh face away; without the compaction their
-// lanes idle through their neighbours' setup and raster loops.
+// entry; `jobs` holds one entry per thread): geometry_front per face, then geometry_job on
+// the front-facing faces inside the clip volume. When fewer than three quarters of the
+// CTA's faces go on (a closed mesh turns about half of its faces away), they are first
+// compacted into `jobs` by warp ballots, so that the second pass runs with every lane
+// busy instead of idling the culled faces' lanes through their neighbours' raster loops;
+// otherwise each thread goes on with its own face (the shared-memory round trip would
+// cost more than the idle lanes).
 __device__ __forceinline__ void geometry_compacted(const DrawParams& p, uint32_t o, DevCounters* c, bool stats,
                                                    FaceJob* jobs, uint32_t* count) {
     GeomStats st = {0, 0, 0, 0};
@@ -343,9 +346,15 @@ __device__ __forceinline__ void geometry_compacted(const DrawParams& p, uint32_t
     uint32_t base = 0;
     if (lane == 0 && m) base = atomicAdd(count, (uint32_t)__popc(m));
     base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (queued) jobs[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = job;
     __syncthreads();
-    if (threadIdx.x < *count) geometry_job(p, jobs[threadIdx.x], st, single_tile);
+    const uint32_t n = *count;
+    if (4u * n >= 3u * blockDim.x) {
+        if (queued) geometry_job(p, job, st, single_tile);
+    } else {
+        if (queued) jobs[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = job;
+        __syncthreads();
+        if (threadIdx.x < n) geometry_job(p, jobs[threadIdx.x], st, single_tile);
+    }
     geometry_warp_tail(p.target, c, stats, st, single_tile);
 }
 
