@@ -639,27 +639,33 @@ __global__ void barrier_probe_kernel(DevCounters* c, unsigned long long timeout_
 
 template <int S>
 cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStream_t stream, cudaEvent_t* ev,
-                           uint64_t* launches) {
+                           uint64_t* launches, bool clear_late) {
     cudaError_t e = cudaMemsetAsync(bp.counters, 0, kBatchCountersReset, stream);
     if (e != cudaSuccess) return e;
     if (form == kFormPhased) {
         auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], stream) : cudaSuccess; };
-        if ((e = mark(0)) != cudaSuccess) return e;
-        if (bp.clear_units) {
-            // at the HBM write rate; running it beside the vertex and face phases (a side
-            // stream) measured no faster, since their key atomics then wait on its writes
+        // at the HBM write rate; running it beside the vertex and face phases of the same
+        // draws (a side stream) measured no faster, since their key atomics then wait on its
+        // writes. The raster phases touch only keys and tile flags, so the clear may also
+        // run just before the tile pass (clear_late).
+        auto clear = [&]() -> cudaError_t {
+            if (!bp.clear_units) return cudaSuccess;
             const unsigned g = min(bp.clear_units, (unsigned)num_sms);
             batch_clear_kernel<<<g, kBatchBlock, 0, stream>>>(bp);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
             *launches += 1;
-        }
+            return cudaGetLastError();
+        };
+        if ((e = mark(0)) != cudaSuccess) return e;
+        if (!clear_late && (e = clear()) != cudaSuccess) return e;
         if ((e = mark(1)) != cudaSuccess) return e;
         if (bp.vert_units) batch_vertex_kernel<S><<<bp.vert_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(2)) != cudaSuccess) return e;
         if (bp.face_units) batch_face_kernel<<<bp.face_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(3)) != cudaSuccess) return e;
         if (bp.face_units) batch_large_kernel<<<(unsigned)num_sms * 5u, kBatchBlock, 0, stream>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(4)) != cudaSuccess) return e;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (clear_late && (e = clear()) != cudaSuccess) return e;
+        if ((e = mark(4)) != cudaSuccess) return e;
         if (bp.tile_units) batch_tile_kernel<S><<<bp.tile_units, kBatchBlock, 0, stream>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(5)) != cudaSuccess) return e;
         *launches += (bp.vert_units ? 1 : 0) + (bp.face_units ? 2 : 0) + (bp.tile_units ? 1 : 0);
@@ -699,13 +705,14 @@ cudaError_t launch_batch_s(const BatchParams& bp, int form, int num_sms, cudaStr
 }  // namespace
 
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
-                         cudaEvent_t* phase_events, uint64_t* launches) {
+                         cudaEvent_t* phase_events, uint64_t* launches, bool clear_late) {
     switch (shader) {
-        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, phase_events, launches);
-        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, phase_events, launches);
-        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, phase_events, launches);
-        case kBlinnPhong: return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, phase_events, launches);
-        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches);
+        case kFlat: return launch_batch_s<kFlat>(bp, form, num_sms, stream, phase_events, launches, clear_late);
+        case kPhong: return launch_batch_s<kPhong>(bp, form, num_sms, stream, phase_events, launches, clear_late);
+        case kPBR: return launch_batch_s<kPBR>(bp, form, num_sms, stream, phase_events, launches, clear_late);
+        case kBlinnPhong:
+            return launch_batch_s<kBlinnPhong>(bp, form, num_sms, stream, phase_events, launches, clear_late);
+        case kGouraud: return launch_batch_s<kGouraud>(bp, form, num_sms, stream, phase_events, launches, clear_late);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -12,10 +12,11 @@ namespace axr {
 // of shader kind `shader`) in launch form `form`: kFormPersistent, one cooperative grid of
 // (resident CTAs per SM) x num_sms CTAs running the four phases; kFormPhased, a clear
 // kernel for the fully cleared draws and then four launches. `phase_events` (optional,
-// 6 events, phased form only) are recorded around the five launches. Adds the number of
-// kernels launched to *launches.
+// 6 events, phased form only) are recorded around the five launches. `clear_late` (phased
+// form, without phase events) runs the clear kernel after the large-triangle phase, right
+// before the tile pass, instead of first. Adds the number of kernels launched to *launches.
 cudaError_t launch_batch(int shader, const BatchParams& bp, int form, int num_sms, cudaStream_t stream,
-                         cudaEvent_t* phase_events, uint64_t* launches);
+                         cudaEvent_t* phase_events, uint64_t* launches, bool clear_late = false);
 
 // Adds the statistics and error bits of `src` (a second launch set's counters) to `dst`
 // and zeroes them in `src` (one thread).

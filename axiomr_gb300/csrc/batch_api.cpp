@@ -334,8 +334,11 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
             ev = &ctx->batch_events[ctx->batch_events_used];
             ctx->batch_events_used += 6;
         }
+        // set 1 clears right before its tile pass: its clear (bound by the write rate) then
+        // meets set 0's latency-bound tile pass, and set 0's clear meets set 1's vertex and
+        // face phases, instead of the two clears meeting each other
         AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, L.set ? side : ctx->stream, ev,
-                                   &ctx->launches));
+                                   &ctx->launches, split && L.set > 0));
     }
     if (b->sets > 1) {
         // set 1's statistics and error bits into the context's counters, which axr_sync and
