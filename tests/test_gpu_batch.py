@@ -355,6 +355,12 @@ def test_split_phased_batch_equals_unsplit(ctx):
                 for k, d in enumerate(draws):
                     assert_same(d.framebuffer.read(), frames[form][k], f"graph replay of the split batch, draw {k}")
                 g.close()
+                for d in draws:  # the one-shot entry point plans and launches the same split
+                    d.framebuffer.clearColor(5, 5, 5, 5)
+                api.draw_batch(ctx, draws)
+                ctx.sync()
+                for k, d in enumerate(draws):
+                    assert_same(d.framebuffer.read(), frames[form][k], f"one-shot split batch, draw {k}")
             batch.close()
     finally:
         ctx.batch_form = saved
