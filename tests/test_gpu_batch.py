@@ -398,3 +398,43 @@ def test_mesh_update_refreshes_bounds_for_planning(ctx):
              api.Draw(mesh_b, fb_b, cam, api.BlinnPhongShader(), model, (0, 0, 0, 255), float("inf"))]
     api.draw_batch(ctx, draws)
     assert_same(fb_a.read(), fb_b.read(), "updated vs created mesh")
+
+
+def test_split_batch_mixed_kinds_and_clears(ctx):
+    """A phased batch of 150 draws of all five shader kinds (five groups, each run as two
+    launch sets) with mixed clear requests (both planes, colour only, none) over
+    framebuffers that start from a known state: every frame equals the persistent form's."""
+    kinds = (W.SHADER_FLAT, W.SHADER_PHONG, W.SHADER_PBR, W.SHADER_BLINN_PHONG, W.SHADER_GOURAUD)
+    base = {kind: W.sphere_scene(width=64, height=48, lon=24, lat=12, tex_size=16, shader=kind) for kind in kinds}
+    scenes = []
+    for k in range(150):
+        kind = kinds[k % 5]
+        sc = base[kind]
+        cam = W.orbit_camera(2.0 + 0.02 * k, 10.0 + k % 40, 7.0 * k, sc.width, sc.height)
+        scenes.append(W.Scene(f"mix{k}", sc.mesh, cam, sc.shader, sc.width, sc.height))
+    draws = api.batch_draws(ctx, scenes)
+    for k, d in enumerate(draws):
+        if k % 3 == 1:
+            d.clear_depth = None
+        elif k % 3 == 2:
+            d.clear_color = None
+            d.clear_depth = None
+    saved = ctx.batch_form
+    frames = {}
+    try:
+        for form in (api.BATCH_PERSISTENT, api.BATCH_PHASED):
+            ctx.batch_form = form
+            batch = api.Batch(ctx, draws)
+            if form == api.BATCH_PHASED:
+                assert batch.info()["launches"] == 10  # five kinds, two launch sets each
+            for d in draws:
+                d.framebuffer.clearColor(40, 50, 60, 70)
+                d.framebuffer.clearDepth(0.9)
+            batch.launch()
+            ctx.sync()
+            frames[form] = [d.framebuffer.read() for d in draws]
+            batch.close()
+    finally:
+        ctx.batch_form = saved
+    for k in range(len(draws)):
+        assert_same(frames[api.BATCH_PHASED][k], frames[api.BATCH_PERSISTENT][k], f"mixed split draw {k}")
