@@ -12,7 +12,7 @@ from . import build as _build
 
 AXR_OK = 0
 STATUS_NAMES = {0: "AXR_OK", 1: "AXR_E_INVALID", 2: "AXR_E_OOM", 3: "AXR_E_BUDGET", 4: "AXR_E_TIMEOUT",
-                5: "AXR_E_CUDA", 6: "AXR_E_UNSUPPORTED", 7: "AXR_E_CAPACITY"}
+                5: "AXR_E_CUDA", 6: "AXR_E_UNSUPPORTED", 7: "AXR_E_CAPACITY", 8: "AXR_E_CANCELLED"}
 
 
 class AxrError(RuntimeError):
@@ -224,6 +224,7 @@ SIGNATURES = {
     "axr_server_wait": (S, [P, C.c_uint64, C.c_int32, P]),
     "axr_server_get_stats": (S, [P, P]),
     "axr_server_hold": (S, [P, C.c_int32]),
+    "axr_server_cancel": (S, [P, C.c_uint64]),
     "axr_server_last_error": (C.c_char_p, [P]),
     "axr_batch_get_form": (C.c_int32, [P]),
     "axr_graph_begin": (S, [P]),

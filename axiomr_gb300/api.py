@@ -740,6 +740,11 @@ class Server:
         self._check(self.lib.axr_server_wait(self.handle, int(ticket), int(timeout_ms), C.byref(res)))
         return {k: getattr(res, k) for k, _ in _lib.ServerResult._fields_}
 
+    def cancel(self, ticket: int) -> None:
+        """Cancel a request still in the queue (axr_server_cancel); its wait() then reports
+        status AXR_E_CANCELLED (8). Raises for a request already in a batch or done."""
+        self._check(self.lib.axr_server_cancel(self.handle, int(ticket)))
+
     def hold(self, on: bool = True) -> None:
         """Stop admitting (requests queue up) / resume admitting the queue as batches."""
         self._check(self.lib.axr_server_hold(self.handle, 1 if on else 0))

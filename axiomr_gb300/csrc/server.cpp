@@ -789,6 +789,27 @@ axr_status axr_server_wait(axr_server* srv, uint64_t ticket, int32_t timeout_ms,
     return AXR_OK;
 }
 
+axr_status axr_server_cancel(axr_server* srv, uint64_t ticket) {
+    if (!srv) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        auto it = srv->reqs.find(ticket);
+        if (it == srv->reqs.end()) return fail(nullptr, AXR_E_INVALID, "unknown ticket %llu", (unsigned long long)ticket);
+        Req* q = it->second.get();
+        if (q->finished) return fail(nullptr, AXR_E_INVALID, "request %llu is done", (unsigned long long)ticket);
+        auto pos = std::find(srv->pending.begin(), srv->pending.end(), q);
+        if (pos == srv->pending.end())
+            return fail(nullptr, AXR_E_INVALID, "request %llu is already in a batch", (unsigned long long)ticket);
+        srv->pending.erase(pos);
+        q->status = AXR_E_CANCELLED;
+        q->done = steady_ns();
+        q->finished = true;
+        ++srv->stats.completed;
+    }
+    srv->cv_done.notify_all();
+    return AXR_OK;
+}
+
 axr_status axr_server_hold(axr_server* srv, int32_t hold) {
     if (!srv) return fail(nullptr, AXR_E_INVALID, "NULL argument");
     {

@@ -27,7 +27,7 @@ extern "C" {
 
 /* Raised whenever a struct or signature of this header changes; a program built against
  * this header can compare it with axr_abi_version() of the library it loaded. */
-#define AXR_ABI_VERSION 2
+#define AXR_ABI_VERSION 3
 int32_t axr_abi_version(void);
 
 /* The reference reports failures with exceptions or silently (src/tiled_pipeline.cpp:146,
@@ -41,7 +41,8 @@ typedef enum axr_status {
     AXR_E_TIMEOUT = 4,     /* a bounded wait gave up */
     AXR_E_CUDA = 5,        /* CUDA runtime error (see axr_last_error) */
     AXR_E_UNSUPPORTED = 6, /* no usable GPU / device capability missing */
-    AXR_E_CAPACITY = 7     /* a preset capacity (faces per draw, captured graph) is too small */
+    AXR_E_CAPACITY = 7,    /* a preset capacity (faces per draw, captured graph) is too small */
+    AXR_E_CANCELLED = 8    /* a serving request was cancelled before it was admitted */
 } axr_status;
 
 /* Shader kinds. FLAT, PHONG and PBR are the reference's FlatShader, PhongShader and
@@ -488,6 +489,11 @@ axr_status axr_server_submit(axr_server* srv, const axr_server_request* req, uin
 /* Wait up to timeout_ms (negative: no limit) for a request; AXR_E_TIMEOUT if not done. */
 axr_status axr_server_wait(axr_server* srv, uint64_t ticket, int32_t timeout_ms, axr_server_result* out);
 axr_status axr_server_get_stats(axr_server* srv, axr_server_stats* out);
+/* Cancel a request that is still queued: it completes at once with AXR_E_CANCELLED (its
+ * host buffers are not touched; axr_server_wait returns that status). A request already
+ * admitted into a batch runs to completion: AXR_E_INVALID, as for an unknown or finished
+ * ticket. */
+axr_status axr_server_cancel(axr_server* srv, uint64_t ticket);
 /* hold != 0: admit nothing (requests queue up; the batches in flight finish); hold == 0:
  * resume, admitting the queue as batches. For draining a node or grouping a burst. */
 axr_status axr_server_hold(axr_server* srv, int32_t hold);

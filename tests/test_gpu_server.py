@@ -166,3 +166,48 @@ def test_png_outputs(ctx, per_request):
     res = srv.wait(t_small, 60000)
     assert res["status"] == 7 and res["png_bytes"] > 64  # AXR_E_CAPACITY
     srv.close()
+
+
+def test_cancel_queued_request():
+    """Host-side fault injection: with admission held, a queued request is cancelled; it
+    completes with AXR_E_CANCELLED and its host buffers stay untouched, the others render
+    normally once admission resumes. Cancelling an unknown or finished ticket fails."""
+    sc = W.sphere_scene(width=96, height=80, lon=16, lat=8, tex_size=16)
+    srv = api.Server(0, budget_bytes=1 << 30, max_batch=8, max_inflight=1)
+    ids = [srv.add_mesh(sc.mesh)]
+    srv.hold(True)
+    reqs = [request(srv, ids, sc, 0) for _ in range(3)]
+    srv.cancel(reqs[1][0])
+    with pytest.raises(AxrError):
+        srv.cancel(reqs[1][0] + 1000)  # unknown ticket
+    srv.hold(False)
+    res = [srv.wait(t, 60000) for t, _, _ in reqs]
+    assert [r["status"] for r in res] == [AXR_OK, 8, AXR_OK]  # AXR_E_CANCELLED
+    assert not reqs[1][1].any() and not reqs[1][2].any()
+    assert np.array_equal(reqs[0][1], reqs[2][1]) and reqs[0][1].any()
+    t, bgra, depth = request(srv, ids, sc, 0)  # the host buffers must outlive the request
+    srv.wait(t, 60000)
+    with pytest.raises(AxrError):
+        srv.cancel(t)  # waited for, so no longer known
+    srv.close()
+    assert bgra.any()
+
+
+def test_slow_consumer_results_are_kept(ctx):
+    """Host-side fault injection: a consumer that collects results late and out of order.
+    The loop keeps running, every result is held until it is waited for, and each equals
+    the per-draw path's frame."""
+    scenes = scenes_mix()
+    srv = api.Server(0, budget_bytes=1 << 30, max_batch=4, max_inflight=2)
+    ids = [srv.add_mesh(sc.mesh) for sc in scenes]
+    reqs = [(k % len(scenes),) + request(srv, ids, scenes[k % len(scenes)], k % len(scenes)) for k in range(21)]
+    order = list(range(len(reqs)))[::-1][:7] + list(range(len(reqs)))[:14]  # the last ones first
+    for i in order:
+        k, t, bgra, depth = reqs[i]
+        assert srv.wait(t, 60000)["status"] == AXR_OK
+    exp = [per_draw(ctx, sc) for sc in scenes]
+    for k, t, bgra, depth in reqs:
+        assert np.array_equal(bgra, exp[k][0])
+        assert np.array_equal(depth.view(np.uint32), exp[k][1].view(np.uint32))
+    assert srv.stats()["completed"] == len(reqs)
+    srv.close()
