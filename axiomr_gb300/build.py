@@ -84,7 +84,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         objs = [f.result() for f in futs]
     tmp = LIB.with_suffix(".so.tmp")
     _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-cudart", "static",
-          "-Xlinker", "--exclude-libs,ALL", "-lpthread", "-ldl", "-lrt"])
+          "-Xlinker", "--exclude-libs,ALL", "-Xlinker", f"--version-script={CSRC / 'exports.map'}",
+          "-lpthread", "-ldl", "-lrt"])
     tmp.replace(LIB)
     (OUT_DIR / "ptxas.log").write_text("\n".join(logs))
     if verbose:

@@ -708,6 +708,7 @@ void axr_readback_destroy(axr_context* ctx, axr_readback* rb) {
 
 axr_status axr_readback_start(axr_context* ctx, axr_readback* rb, int32_t count, const axr_framebuffer* const* fbs,
                               uint8_t* const* bgra, float* const* depth) {
+    NvtxRange nvtx_range("axr_readback_start");
     if (!ctx || !rb || count < 0 || (count > 0 && !fbs)) return fail(ctx, AXR_E_INVALID, "bad read-back arguments");
     if (rb->device != ctx->device) return fail(ctx, AXR_E_INVALID, "the read-back belongs to another device");
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -729,6 +730,7 @@ axr_status axr_readback_start(axr_context* ctx, axr_readback* rb, int32_t count,
 axr_status axr_readback_start_packed(axr_context* ctx, axr_readback* rb, int32_t count,
                                      const axr_framebuffer* const* fbs, int32_t format, uint8_t* host,
                                      uint64_t capacity) {
+    NvtxRange nvtx_range("axr_readback_start_packed");
     if (!ctx || !rb || count < 0 || (count > 0 && (!fbs || !host))) return fail(ctx, AXR_E_INVALID, "bad read-back arguments");
     if (format != AXR_PACKED_BGRA && format != AXR_PACKED_RGB) return fail(ctx, AXR_E_INVALID, "unknown format %d", format);
     if (rb->device != ctx->device) return fail(ctx, AXR_E_INVALID, "the read-back belongs to another device");
@@ -855,6 +857,7 @@ axr_status axr_set_framebuffer(axr_context* ctx, axr_framebuffer* fb) {
 }
 
 axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float model[16]) {
+    NvtxRange nvtx_range("axr_draw_mesh");
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     if (!mesh || !model) return fail(ctx, AXR_E_INVALID, "NULL mesh or model matrix");
     std::lock_guard<std::mutex> lk(ctx->mu);

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "api_types.h"
 
 namespace axr {
@@ -16,6 +18,15 @@ struct PackedImage {
 }
 
 namespace axr_internal {
+
+// NVTX range over a host entry point, so that a timeline tool shows the library's calls
+// beside their kernels (a few nanoseconds when no tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Record a formatted message as the context's last error (or the thread's, without a
 // context) and return `st`.

@@ -433,6 +433,7 @@ void free_batch_staging(axr_batch* b) {
 extern "C" {
 
 axr_status axr_batch_create(axr_context* ctx, const axr_draw_desc* draws, int32_t count, axr_batch** out) {
+    NvtxRange nvtx_range("axr_batch_create");
     if (!ctx || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
     *out = nullptr;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -449,6 +450,7 @@ axr_status axr_batch_create(axr_context* ctx, const axr_draw_desc* draws, int32_
 }
 
 axr_status axr_batch_launch(axr_context* ctx, axr_batch* b) {
+    NvtxRange nvtx_range("axr_batch_launch");
     if (!ctx || !b) return fail(ctx, AXR_E_INVALID, "NULL argument");
     if (b->device != ctx->device) return fail(ctx, AXR_E_INVALID, "batch planned for another device");
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -479,6 +481,7 @@ axr_status axr_batch_get_info(const axr_batch* b, axr_batch_info* out) {
 }
 
 axr_status axr_draw_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t count) {
+    NvtxRange nvtx_range("axr_draw_batch");
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (ctx->capturing) return fail(ctx, AXR_E_INVALID, "axr_draw_batch cannot be captured; capture axr_batch_launch");
@@ -509,6 +512,7 @@ axr_status axr_batch_set_tuning(axr_context* ctx, const int32_t small_max_pixels
 
 axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int32_t count, int32_t repeats,
                               int32_t out_small_max_pixels[AXR_TUNE_CLASSES]) {
+    NvtxRange nvtx_range("axr_batch_autotune");
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     if (repeats < 1) repeats = 1;
     axr_status st = check_draws(ctx, draws, count);

@@ -982,6 +982,7 @@ extern "C" uint64_t axr_png_bound(uint32_t width, uint32_t height, uint32_t chan
 extern "C" axr_status axr_framebuffers_encode_png(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
                                                   uint32_t channels, void* const* out, const uint64_t* capacity,
                                                   uint64_t* sizes) {
+    NvtxRange nvtx_range("axr_framebuffers_encode_png");
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);
     DeviceGuard g(ctx->device);
@@ -1164,6 +1165,7 @@ extern "C" void axr_png_batch_destroy(axr_context* ctx, axr_png_batch* b) {
 
 extern "C" axr_status axr_png_batch_encode(axr_context* ctx, axr_png_batch* b, int32_t count,
                                            const axr_framebuffer* const* fbs, uint32_t channels) {
+    NvtxRange nvtx_range("axr_png_batch_encode");
     if (!ctx || !b) return fail(ctx, AXR_E_INVALID, "NULL argument");
     if (b->device != ctx->device) return fail(ctx, AXR_E_INVALID, "the PNG batch belongs to another device");
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1185,6 +1187,7 @@ extern "C" axr_status axr_png_batch_read(axr_context* ctx, axr_png_batch* b, voi
 extern "C" axr_status axr_framebuffers_read_png(axr_context* ctx, int32_t count, const axr_framebuffer* const* fbs,
                                                 uint32_t channels, void* const* files, const uint64_t* capacity,
                                                 uint64_t* sizes) {
+    NvtxRange nvtx_range("axr_framebuffers_read_png");
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     if (count < 0 || (count > 0 && (!fbs || !sizes))) return fail(ctx, AXR_E_INVALID, "bad framebuffer list");
     if (channels != 3 && channels != 4) return fail(ctx, AXR_E_INVALID, "channels must be 3 (RGB) or 4 (RGBA)");

@@ -284,6 +284,7 @@ unsigned grid(size_t n) { return (unsigned)std::max<size_t>(1, (n + kBlock - 1) 
 }  // namespace
 
 extern "C" axr_status axr_mesh_create_from_obj(axr_context* ctx, const axr_obj_desc* d, axr_mesh** out) {
+    NvtxRange nvtx_range("axr_mesh_create_from_obj");
     if (!ctx || !d || !out) return fail(ctx, AXR_E_INVALID, "NULL argument");
     *out = nullptr;
     if ((d->num_positions && !d->positions) || (d->num_uvs && !d->uvs) || (d->num_normals && !d->normals) ||

@@ -25,6 +25,7 @@
 
 #include <mutex>
 
+#include "api_internal.h"
 #include "api_types.h"
 
 namespace {
@@ -73,6 +74,7 @@ axr_status noalloc_fail(axr_context* ctx, axr_status st, const std::string& msg)
 }  // namespace
 
 extern "C" axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* mesh, const float model[16]) {
+    axr_internal::NvtxRange nvtx_range("axr_draw_mesh_noalloc");
     if (!ctx) return AXR_E_INVALID;
     if (!mesh || !model) return noalloc_fail(ctx, AXR_E_INVALID, "NULL mesh or model matrix");
     std::lock_guard<std::mutex> lk(ctx->mu);

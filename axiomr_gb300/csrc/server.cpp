@@ -407,6 +407,7 @@ struct axr_server {
 
     // ---------------------------------------------------------------- batches
     axr_status launch(Slot& s) {
+    NvtxRange nvtx_range("axr_server batch");
         const uint64_t t = steady_ns();
         for (Req* q : s.reqs) q->launch = t;
         cudaError_t e = cudaSuccess;
