@@ -438,3 +438,32 @@ def test_split_batch_mixed_kinds_and_clears(ctx):
         ctx.batch_form = saved
     for k in range(len(draws)):
         assert_same(frames[api.BATCH_PHASED][k], frames[api.BATCH_PERSISTENT][k], f"mixed split draw {k}")
+
+
+def test_full_mixed_batch_split_equals_persistent(ctx):
+    """The benchmark's 512-draw mixed batch (framebuffers at half scale, 1024² textures):
+    the phased form, split into two launch sets, gives every frame of the persistent form
+    bit for bit; compared through per-frame digests of colour and depth."""
+    import hashlib
+
+    scenes = W.batch_scenes(count=512, tex_size=1024, resolution_scale=0.5)
+    draws = api.batch_draws(ctx, scenes)
+    saved = ctx.batch_form
+    digests = {}
+    try:
+        for form in (api.BATCH_PERSISTENT, api.BATCH_PHASED):
+            ctx.batch_form = form
+            batch = api.Batch(ctx, draws)
+            assert batch.info()["launches"] == (2 if form == api.BATCH_PHASED else 1)
+            batch.launch()
+            ctx.sync()
+            out = []
+            for d in draws:
+                bgra, depth = d.framebuffer.read()
+                out.append(hashlib.sha1(bgra.tobytes() + np.ascontiguousarray(depth).view(np.uint32).tobytes()).digest())
+            digests[form] = out
+            batch.close()
+    finally:
+        ctx.batch_form = saved
+    bad = [k for k in range(len(draws)) if digests[api.BATCH_PHASED][k] != digests[api.BATCH_PERSISTENT][k]]
+    assert not bad, f"{len(bad)} draws differ, first {bad[:5]}"
