@@ -34,6 +34,12 @@ constexpr int kBatchWarps = kBatchBlock / 32;
 constexpr int kBatchMinBlocks = 3;  // 256 threads x 3 CTAs: at most 85 registers
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
 
+// Resident 256-thread CTAs per SM the phased face kernel is compiled for (5: at most 51
+// registers; its shared memory, 15 KB per CTA, allows more).
+#ifndef AXR_FACE_MIN_BLOCKS
+#define AXR_FACE_MIN_BLOCKS 5
+#endif
+
 // Resident 256-thread CTAs per SM the phased tile kernel is compiled for (4: at most 64
 // registers; its shared memory, 36 KB per CTA, allows 6).
 #ifndef AXR_TILE_MIN_BLOCKS
@@ -480,7 +486,7 @@ __global__ void __launch_bounds__(kBatchBlock) batch_vertex_kernel(const __grid_
     vertex_unit<S>(s_p, s_u);
 }
 
-__global__ void __launch_bounds__(kBatchBlock, 5) batch_face_kernel(const __grid_constant__ BatchParams bp) {
+__global__ void __launch_bounds__(kBatchBlock, AXR_FACE_MIN_BLOCKS) batch_face_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ __align__(16) DrawParams s_p;
     __shared__ UnitInfo s_u;
     __shared__ FaceJob s_jobs[kBatchBlock];
