@@ -81,6 +81,10 @@ def parse_args():
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: device-memory residency budget")
     ap.add_argument("--readback", choices=("colour", "png", "none"), default="colour",
                     help="serve: read each request's colour plane back to host memory, or not")
+    ap.add_argument("--serve-mix", choices=("soup", "c4"), default="soup",
+                    help="serve: common requests are 3840x2160 soups, or draws of the mixed batch")
+    ap.add_argument("--brief-serve-seconds", type=float, default=2.0,
+                    help="batch: seconds per offered load of the short serving sweep in the line (0: none)")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -473,6 +477,18 @@ def timed_steps(stream, flush, steps: int, body):
     return [a.elapsed_time(b) for a, b in evs]
 
 
+def batch_config(args, dist: "Dist", frames: int) -> dict:
+    """The mixed-batch workload as both arms describe it (identical dictionaries, so that
+    the two lines name the same configuration); how each arm renders it is reported
+    outside `config`."""
+    desc = WORKLOADS["batch"][1]
+    if args.draws != 512 or args.scale != 1.0:
+        desc += f" [reduced: first {args.draws} draws, framebuffers scaled by {args.scale}]"
+    return {"workload": f"batch: {desc}", "frames_per_step": frames, "draws": args.draws, "resolution_scale": args.scale,
+            "l2": "flushed before every timed step (256 MiB write, outside the events); inputs larger than L2",
+            "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"}
+
+
 def batch_algo_bytes(scenes, frags: float) -> float:
     """Algorithmic bytes of one mixed-batch step: per draw the vertex attributes read
     (position 12 + normal 12 + uv 8), the indices (12 per face), one colour + one depth
@@ -597,10 +613,7 @@ def run_batch(args, dist: Dist):
 
     from axiomr_gb300 import api
 
-    desc = WORKLOADS["batch"][1]
     scenes = W.batch_scenes(count=args.draws, resolution_scale=args.scale)
-    if args.draws != 512 or args.scale != 1.0:
-        desc += f" [reduced: first {args.draws} draws, framebuffers scaled by {args.scale}]"
     dev = dist.local_rank
     torch.cuda.set_device(dev)
     ctx = api.Context(dev)
@@ -797,17 +810,15 @@ def run_batch(args, dist: Dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
-        "config": {"workload": f"batch: {desc}",
-                   "form": ("batched, phased: a clear kernel and four phase launches over the work units of "
-                            "all draws, as two launch sets of alternating draws on two streams"
-                            if info["form"] == 1 and info["launches"] > 1 else
-                            "batched, phased: a clear kernel and four phase launches per step over the work "
-                            "units of all draws" if info["form"] == 1 else
-                            "batched, persistent: one cooperative launch per step (clears fused into the tile pass)")
-                   + ", replayed from a CUDA graph",
-                   "frames_per_step": n, "l2": "flushed before every timed step (256 MiB write, outside the events)",
-                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
-                   "tuning_small_max_pixels": tuning},
+        "config": batch_config(args, dist, n),
+        "form_desc": ("batched, phased: a clear kernel and four phase launches over the work units of "
+                      "all draws, as two launch sets of alternating draws on two streams"
+                      if info["form"] == 1 and info["launches"] > 1 else
+                      "batched, phased: a clear kernel and four phase launches per step over the work "
+                      "units of all draws" if info["form"] == 1 else
+                      "batched, persistent: one cooperative launch per step (clears fused into the tile pass)")
+        + ", replayed from a CUDA graph",
+        "tuning_small_max_pixels": tuning,
         "gfrag_per_s": round(frags * value / n / 1e9, 3),
         "mtri_per_s": round(faces * value / n / 1e6, 2),
         "fragments_per_step": int(frags), "shaded_per_step": int(st["shaded"]), "tested_per_step": int(st["tested"]),
@@ -821,6 +832,10 @@ def run_batch(args, dist: Dist):
         "batched_vs_plain": round(value / plain_value, 3),
         "e2e": {"value": round(e2e_value, 2), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
+                # the device-resident comparison the batched form is built for, kept as plain
+                # numbers beside the end-to-end figure
+                "plain_frames_per_s": round(plain_value, 2), "batched_frames_per_s": round(value, 2),
+                "batched_vs_plain": round(value / plain_value, 3),
                 "path": "per step axr_draw_batch (draw table from the host) + read-back of all 512 rendered "
                         "images (BGRA8 colour planes, as stored) into one pinned buffer: gathered on the device "
                         "and copied as one block (axr_readback_start_packed / axr_readback_wait), pipelined over "
@@ -866,65 +881,78 @@ def run_batch(args, dist: Dist):
     return out, scenes
 
 
-def run_serve(args, dist: Dist):
+def serve_sweep(device: int, rates, seconds: float, budget_gb: float, readback: str = "colour", mix: str = "soup",
+                n_assets: int = 64, seed: int = 6) -> dict:
     """Serving loop under open-loop Poisson load: per offered rate, p50/p99 latency (arrival
     to colour read-back done, server clock) and achieved frames/s, for the batched loop and
-    for the same loop rendering every request alone with the per-draw path."""
+    for the same loop rendering every request alone with the per-draw path.
+
+    mix "soup": 90% requests of the small-triangle configuration (a 200,000-triangle soup at
+    3840x2160, Gouraud, one of `n_assets` seeded soups), 10% heightfields (1920x1080,
+    Blinn-Phong, random camera azimuth). mix "c4": 90% requests drawn from the mixed batch's
+    per-draw distribution (a random draw of the 512-draw plan: its sphere, resolution,
+    camera and texture), 10% heightfields."""
     from axiomr_gb300 import api
 
-    desc = WORKLOADS["serve"][1]
-    rng = np.random.default_rng(6)
-    soups = [W.soup_scene(seed=1000 + k) for k in range(64)]
+    rng = np.random.default_rng(seed)
     hf = W.heightfield_scene()
-    rates = [float(r) for r in args.rates.split(",") if r]
-    cam_soup = api.Camera.from_workload(soups[0].camera)
+    if mix == "soup":
+        common = [W.soup_scene(seed=1000 + k) for k in range(n_assets)]
+    else:
+        common = W.batch_scenes()
     gouraud, blinn = api.GouraudShader(), api.BlinnPhongShader()
     out_modes = {}
     for mode in ("batched", "per_request"):
-        srv = api.Server(dist.local_rank, budget_bytes=int(args.budget_gb * (1 << 30)), max_batch=64, max_inflight=2,
+        srv = api.Server(device, budget_bytes=int(budget_gb * (1 << 30)), max_batch=64, max_inflight=2,
                          per_request=(mode == "per_request"))
-        soup_ids = [srv.add_mesh(sc.mesh) for sc in soups]
+        mesh_ids = {}
+        for sc in common:
+            if id(sc.mesh) not in mesh_ids:
+                mesh_ids[id(sc.mesh)] = srv.add_mesh(sc.mesh)
+        reqs = [(mesh_ids[id(sc.mesh)], api.Camera.from_workload(sc.camera),
+                 gouraud if sc.shader.kind == W.SHADER_GOURAUD else blinn, sc.width, sc.height) for sc in common]
         hf_id = srv.add_mesh(hf.mesh)
         # pinned colour buffers, reused round robin by the requests in flight
-        ring = []
         keep = []
         lib = srv.lib
-        if args.readback == "colour":
-            ring = [pinned_bytes(lib, 3840 * 2160 * 4, keep).reshape(2160, 3840, 4) for _ in range(96)]
-            hf_ring = [pinned_bytes(lib, 1920 * 1080 * 4, keep).reshape(1080, 1920, 4) for _ in range(16)]
-        elif args.readback == "png":  # RGB PNG files encoded on the GPU instead of the raw plane
-            ring = [pinned_bytes(lib, api.png_bound(3840, 2160, 3), keep) for _ in range(96)]
+        big = max(sc.width * sc.height for sc in common)
+        if readback == "colour":
+            ring = [pinned_bytes(lib, big * 4, keep) for _ in range(96)]
+            hf_ring = [pinned_bytes(lib, 1920 * 1080 * 4, keep) for _ in range(16)]
+        elif readback == "png":  # RGB PNG files encoded on the GPU instead of the raw plane
+            cap = max(api.png_bound(sc.width, sc.height, 3) for sc in common)
+            ring = [pinned_bytes(lib, cap, keep) for _ in range(96)]
             hf_ring = [pinned_bytes(lib, api.png_bound(1920, 1080, 3), keep) for _ in range(16)]
         else:
             ring, hf_ring = [None], [None]
 
         def out(buf):
-            return {"png_channels": 3, "out_png": buf} if args.readback == "png" else {"out_bgra": buf}
+            return {"png_channels": 3, "out_png": buf} if readback == "png" else {"out_bgra": buf}
 
         # warm-up: every asset resident once, framebuffer pools filled
-        ts = [srv.submit(i, cam_soup, gouraud, 3840, 2160, **out(ring[k % len(ring)])) for k, i in enumerate(soup_ids)]
+        ts = [srv.submit(*r, **out(ring[k % len(ring)])) for k, r in enumerate(reqs)]
         ts.append(srv.submit(hf_id, api.Camera.from_workload(hf.camera), blinn, 1920, 1080, **out(hf_ring[0])))
         for t in ts:
             srv.wait(t)
         per_rate = []
         for rate in rates:
-            n = max(1, int(rate * args.serve_seconds))
+            n = max(1, int(rate * seconds))
             gaps = rng.exponential(1.0 / rate, n)
             offs = (np.cumsum(gaps) * 1e9).astype(np.int64)
             kinds = rng.random(n) < 0.9
-            which = rng.integers(0, len(soup_ids), n)
+            which = rng.integers(0, len(reqs), n)
             az = rng.random(n) * 360.0
             tickets = [None] * n
             t0 = srv.now_ns() + 2_000_000
             k = 0
-            soup_slot = hf_slot = 0
+            slot = hf_slot = 0
             while k < n:
                 now = srv.now_ns()
                 while k < n and t0 + int(offs[k]) <= now:
                     if kinds[k]:
-                        tickets[k] = srv.submit(soup_ids[which[k]], cam_soup, gouraud, 3840, 2160,
-                                                arrival_ns=t0 + int(offs[k]), **out(ring[soup_slot % len(ring)]))
-                        soup_slot += 1
+                        tickets[k] = srv.submit(*reqs[which[k]], arrival_ns=t0 + int(offs[k]),
+                                                **out(ring[slot % len(ring)]))
+                        slot += 1
                     else:
                         c = W.orbit_camera(2.5, 30.0, float(az[k]), 1920, 1080)
                         tickets[k] = srv.submit(hf_id, api.Camera.from_workload(c), blinn, 1920, 1080,
@@ -935,7 +963,7 @@ def run_serve(args, dist: Dist):
                     wait = (t0 + int(offs[k]) - srv.now_ns()) / 1e9
                     if wait > 2e-4:
                         time.sleep(wait - 1e-4)
-            lat, sizes, first, last, fails = [], [], None, 0, 0
+            lat, sizes, last, fails = [], [], 0, 0
             for t in tickets:
                 r = srv.wait(t)
                 if r["status"] != 0:
@@ -951,28 +979,52 @@ def run_serve(args, dist: Dist):
                              "p50_ms": round(float(np.percentile(lat, 50)), 3) if lat.size else None,
                              "p99_ms": round(float(np.percentile(lat, 99)), 3) if lat.size else None,
                              "mean_batch": round(float(np.mean(sizes)), 2) if sizes else None})
-            print(json.dumps({"mode": mode, **per_rate[-1]}), file=sys.stderr, flush=True)
+            print(json.dumps({"mix": mix, "mode": mode, **per_rate[-1]}), file=sys.stderr, flush=True)
         st = srv.stats()
         srv.close()
         for p in keep:
             lib.axr_host_free(p)
         out_modes[mode] = {"rates": per_rate, "uploads": st["uploads"], "evictions": st["evictions"],
                            "framebuffers": st["framebuffers"], "peak_resident_gb": round(st["peak_bytes"] / 2**30, 2)}
-    top = out_modes["batched"]["rates"][-1]
+    return out_modes
+
+
+def serve_scalars(modes: dict, prefix: str = "serve") -> dict:
+    """Flat per-rate figures of a serving sweep (p50/p99 of both modes, achieved frames/s)."""
+    out = {}
+    for mode, tag in (("batched", "batched"), ("per_request", "per_req")):
+        for r in modes[mode]["rates"]:
+            rps = int(r["offered_rps"])
+            out[f"{prefix}_{tag}_p50_ms_{rps}rps"] = r["p50_ms"]
+            out[f"{prefix}_{tag}_p99_ms_{rps}rps"] = r["p99_ms"]
+            out[f"{prefix}_{tag}_fps_{rps}rps"] = r["achieved_fps"]
+    return out
+
+
+def run_serve(args, dist: Dist):
+    desc = WORKLOADS["serve"][1]
+    rates = [float(r) for r in args.rates.split(",") if r]
+    modes = serve_sweep(dist.local_rank, rates, args.serve_seconds, args.budget_gb, args.readback, args.serve_mix)
+    top = modes["batched"]["rates"][-1]
+    if args.serve_mix == "c4":
+        desc = desc.replace("requests of the small-triangle configuration (200,000 triangles, 3840x2160, Gouraud; "
+                            "one of 64 seeded soups)", "requests drawn from the mixed batch's per-draw distribution")
     return {
         "metric": "frames/s", "value": top["achieved_fps"], "unit": "frames/s", "n_gpus": dist.world,
         "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
         "config": {"workload": f"serve: {desc}", "seconds_per_rate": args.serve_seconds, "max_batch": 64,
-                   "max_inflight": 2, "budget_gb": args.budget_gb, "readback": args.readback},
-        "serving": out_modes,
+                   "max_inflight": 2, "budget_gb": args.budget_gb, "readback": args.readback,
+                   "mix": args.serve_mix},
+        "serving": modes,
     }
 
 
 def cpu_batch_sample(scenes, budget_s: float, steps: int):
     """The CPU restatement of the reference pipeline (oracle/port) on every 32nd draw of the
     mixed batch, all host threads; frames/s over those draws (clears included, as the
-    reference renderer's frame)."""
+    reference renderer's frame). The `cpu_baseline` figure of our arm's line: a bounded
+    sample, so that the GPU run stays short."""
     from oracle import Oracle
 
     port = Oracle("port")
@@ -1001,15 +1053,36 @@ def cpu_batch_sample(scenes, budget_s: float, steps: int):
 def run_reference(args, dist: Dist):
     make, desc = WORKLOADS[args.workload]
     if args.workload == "batch":
-        scenes = make()
-        value, threads, times, sample = cpu_batch_sample(scenes, 150.0, args.steps)
+        # every step renders every draw of the batch (the same configuration as our arm),
+        # with the same warm-up and step counts
+        from oracle import Oracle
+
+        scenes = W.batch_scenes(count=args.draws, resolution_scale=args.scale)
+        port = Oracle("port")
+        threads = os.cpu_count() or 1
+        vps = [port.camera(sc.camera)[2] for sc in scenes]
+
+        def step():
+            for sc, vp in zip(scenes, vps):
+                port.draw(sc, vp, threads=threads)
+
+        for _ in range(args.warmup):
+            step()
+        times = []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            step()
+            times.append(time.perf_counter() - t)
+        value = len(scenes) * len(times) / sum(times)
+        sample = (f"{args.steps} steps of all {len(scenes)} draws after {args.warmup} warm-up steps, one drawMesh "
+                  f"per draw (clears included), on {threads} host threads ({os.uname().machine})")
         return {
             "metric": "frames/s", "value": round(value, 4), "unit": "frames/s", "n_gpus": dist.world,
-            "steps": len(times), "warmup": 1, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
-            "config": {"workload": f"batch: {desc}", "form": "reference CPU TiledPipeline (C restatement), "
-                       "one drawMesh per draw"},
+            "config": batch_config(args, dist, len(scenes)),
+            "form_desc": "reference CPU TiledPipeline (C restatement in oracle/port), one drawMesh per draw",
             "impl": "reference",
             "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
                              "sample": sample},
@@ -1072,6 +1145,15 @@ def main():
             return
         if args.workload == "batch":
             out, scenes = run_batch(args, dist)
+            if args.brief_serve_seconds > 0 and args.draws == 512 and args.scale == 1.0:
+                # a short serving sweep (the metric's p50/p99 request latency per offered
+                # load), its flat figures kept beside the end-to-end number
+                rates = [float(r) for r in args.rates.split(",") if r]
+                modes = serve_sweep(dist.local_rank, rates, args.brief_serve_seconds, args.budget_gb, "colour",
+                                    "soup", n_assets=16)
+                out["serving"] = {"mix": "soup", "seconds_per_rate": args.brief_serve_seconds, "assets": 16,
+                                  "modes": modes}
+                out["e2e"].update(serve_scalars(modes))
             if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
                 value, threads, times, sample = cpu_batch_sample(scenes, args.cpu_budget_s, args.steps)
                 out["cpu_baseline"] = {"value": round(value, 4), "unit": "frames/s", "cores": threads,
