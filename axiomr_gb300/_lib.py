@@ -58,6 +58,11 @@ class DrawDesc(C.Structure):
 
 
 AXR_BATCH_PERSISTENT = 0
+
+
+class BinParams(C.Structure):
+    """axr_bin_params: entries per bin, bin shape (tiles across and down), per-thread raster limit."""
+    _fields_ = [("capacity", C.c_int32), ("tiles_x", C.c_int32), ("thread_pixels", C.c_int32), ("tiles_y", C.c_int32)]
 AXR_BATCH_PHASED = 1
 
 
@@ -227,6 +232,12 @@ SIGNATURES = {
     "axr_server_cancel": (S, [P, C.c_uint64]),
     "axr_server_last_error": (C.c_char_p, [P]),
     "axr_batch_get_form": (C.c_int32, [P]),
+    "axr_set_draw_form": (S, [P, C.c_int32]),
+    "axr_get_draw_form": (C.c_int32, [P]),
+    "axr_set_bin_params": (S, [P, P]),
+    "axr_get_bin_params": (S, [P, P]),
+    "axr_batch_get_bin_tuning": (S, [P, P]),
+    "axr_batch_set_bin_tuning": (S, [P, P]),
     "axr_graph_begin": (S, [P]),
     "axr_graph_end": (S, [P, PP]),
     "axr_graph_launch": (S, [P, P]),

@@ -27,7 +27,8 @@ from ._lib import (AXR_DRAW_CLEAR_COLOR, AXR_DRAW_CLEAR_DEPTH, AXR_TUNE_CLASSES,
                    DrawDesc, DrawStats, GroupDesc, MaterialDesc, MeshDesc, ShaderDesc, check)
 
 FLAT, PHONG, PBR, BLINN_PHONG, GOURAUD = 0, 1, 2, 3, 4
-BATCH_PERSISTENT, BATCH_PHASED = 0, 1  # launch forms of the batched kernel (AXR_BATCH_*)
+BATCH_PERSISTENT, BATCH_PHASED, BATCH_BINNED = 0, 1, 2  # launch forms of the batched kernels (AXR_BATCH_*)
+DRAW_BINNED, DRAW_KEYED = 0, 1  # forms of the per-draw path (AXR_DRAW_*)
 
 
 def _f32(a) -> np.ndarray:
@@ -106,6 +107,41 @@ class Context:
     def set_tuning(self, small_max_pixels: Sequence[int]) -> None:
         arr = (C.c_int32 * AXR_TUNE_CLASSES)(*[int(v) for v in small_max_pixels])
         check(self.lib.axr_batch_set_tuning(self.handle, arr), self.handle)
+
+    @property
+    def draw_form(self) -> int:
+        """Form of the per-draw path (DRAW_BINNED, the default, or DRAW_KEYED)."""
+        return int(self.lib.axr_get_draw_form(self.handle))
+
+    @draw_form.setter
+    def draw_form(self, form: int) -> None:
+        check(self.lib.axr_set_draw_form(self.handle, int(form)), self.handle)
+
+    @property
+    def bin_params(self) -> dict:
+        """Bin parameters of the per-draw binned form (capacity 0: sized per draw)."""
+        b = _lib.BinParams()
+        check(self.lib.axr_get_bin_params(self.handle, C.byref(b)), self.handle)
+        return {"capacity": b.capacity, "tiles_x": b.tiles_x, "tiles_y": b.tiles_y, "thread_pixels": b.thread_pixels}
+
+    @bin_params.setter
+    def bin_params(self, v: dict) -> None:
+        b = _lib.BinParams(int(v.get("capacity", 0)), int(v.get("tiles_x", 0)), int(v.get("thread_pixels", 64)),
+                           int(v.get("tiles_y", 0)))
+        check(self.lib.axr_set_bin_params(self.handle, C.byref(b)), self.handle)
+
+    def bin_tuning(self) -> list:
+        """The binned batch form's bin parameters per density class."""
+        arr = (_lib.BinParams * AXR_TUNE_CLASSES)()
+        check(self.lib.axr_batch_get_bin_tuning(self.handle, arr), self.handle)
+        return [{"capacity": b.capacity, "tiles_x": b.tiles_x, "tiles_y": b.tiles_y, "thread_pixels": b.thread_pixels}
+                for b in arr]
+
+    def set_bin_tuning(self, table: Sequence[dict]) -> None:
+        arr = (_lib.BinParams * AXR_TUNE_CLASSES)(
+            *[_lib.BinParams(int(v["capacity"]), int(v["tiles_x"]), int(v["thread_pixels"]), int(v.get("tiles_y", 0)))
+              for v in table])
+        check(self.lib.axr_batch_set_bin_tuning(self.handle, arr), self.handle)
 
     def close(self) -> None:
         if getattr(self, "handle", None):

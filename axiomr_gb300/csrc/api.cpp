@@ -100,6 +100,17 @@ void free_scratch(axr_context* ctx) {
     ctx->large_cap = ctx->item_cap = ctx->vcap = ctx->px_cap = ctx->rec_cap = 0;
 }
 
+void free_bins(axr_context* ctx) {
+    dfree(ctx->bin_mem);
+    dfree(ctx->bin_entries);
+    dfree(ctx->bin_crec);
+    ctx->bin_mem = nullptr;
+    ctx->bin_entries = nullptr;
+    ctx->bin_crec = nullptr;
+    ctx->bin_count_cap = ctx->crec_cap = 0;
+    ctx->bin_entry_cap = 0;
+}
+
 axr_status grow_scratch(axr_context* ctx, uint32_t faces, uint32_t vertices, uint64_t pixels) {
     // Large-triangle setups and tile work items (a triangle that finds either list full is
     // rasterised by its own thread instead, so those two sizes trade memory for speed), the
@@ -197,6 +208,62 @@ void free_mesh(axr_mesh* m) {
     delete m;
 }
 
+// Scratch of the binned per-draw form: bin counters and counts for `bins` bins, `entries`
+// bin entries and `crec` clipped-triangle records (grown, never shrunk).
+axr_status grow_bins(axr_context* ctx, uint32_t bins, size_t entries, uint32_t crec) {
+    if (bins <= ctx->bin_count_cap && entries <= ctx->bin_entry_cap && crec <= ctx->crec_cap) return AXR_OK;
+    if (ctx->capturing)
+        return fail(ctx, AXR_E_CAPACITY,
+                    "bin scratch for %u bins / %zu entries / %u clipped records not reserved before graph capture "
+                    "(reserved %u / %zu / %u)", bins, entries, crec, ctx->bin_count_cap, ctx->bin_entry_cap,
+                    ctx->crec_cap);
+    bins = std::max(bins, ctx->bin_count_cap);
+    entries = std::max(entries, ctx->bin_entry_cap);
+    crec = std::max(crec, ctx->crec_cap);
+    AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    free_bins(ctx);
+    AXR_CUDA(ctx, cudaMalloc(&ctx->bin_mem, sizeof(BinCounters) + sizeof(uint32_t) * (size_t)bins));
+    AXR_CUDA(ctx, dmalloc(&ctx->bin_entries, entries));
+    AXR_CUDA(ctx, dmalloc(&ctx->bin_crec, (size_t)kRasterRec * crec));
+    ctx->bin_count_cap = bins;
+    ctx->bin_entry_cap = entries;
+    ctx->crec_cap = crec;
+    return AXR_OK;
+}
+
+// Bin shape and capacity of a binned draw of `faces` faces into `fb`.
+struct BinPlan {
+    uint16_t bins_x, bins_y;
+    uint8_t tw, th;
+    uint32_t cap, crec;
+    uint32_t bins() const { return (uint32_t)bins_x * bins_y; }
+};
+
+BinPlan plan_bins(const axr_bin_params& bp, const axr_framebuffer* fb, uint32_t faces) {
+    BinPlan b{};
+    if (bp.tiles_x > 0) {
+        bin_shape(bp, &b.tw, &b.th);
+    } else {  // about 2,400 or more bins (16 per SM of a GB300), 1 to 8 tiles each
+        const uint32_t tiles = (uint32_t)fb->tiles_x * (uint32_t)fb->tiles_y;
+        uint32_t nt = 1;
+        while (nt < 8 && tiles / (2 * nt) >= 2432) nt *= 2;
+        b.tw = (uint8_t)(nt >= 2 ? 2 : 1) * (uint8_t)(nt == 8 ? 2 : 1);
+        b.th = (uint8_t)(nt / b.tw);
+    }
+    bin_geometry(fb->tiles_x, fb->tiles_y, b.tw, b.th, &b.bins_x, &b.bins_y);
+    if (bp.capacity > 0) {
+        b.cap = (uint32_t)bp.capacity;
+    } else {  // twice the mean entries per bin, a power of two in [64, 16384]; the entries of
+              // a denser bin spill through the key plane, which spreads them over all threads
+        const uint64_t mean = 2ull * faces / std::max<uint32_t>(1, b.bins());
+        uint32_t c = 64;
+        while (c < mean && c < 16384) c <<= 1;
+        b.cap = c;
+    }
+    b.crec = std::max<uint32_t>(1u << 16, faces / 4);
+    return b;
+}
+
 DrawParams make_params(axr_context* ctx, const axr_mesh* m, const axr_framebuffer* fb, const DevUniforms& u) {
     DrawParams p{};
     p.mesh = DevMesh{m->pos, m->nrm, m->tan, m->bit, m->uv, m->idx, m->groups, m->materials,
@@ -287,6 +354,7 @@ void axr_context_destroy(axr_context* ctx) {
     dfree(ctx->counters);
     dfree(ctx->batch_prof);
     free_scratch(ctx);
+    free_bins(ctx);
     free_png(ctx);
     if (ctx->aux.stream) cudaStreamSynchronize(ctx->aux.stream);
     if (ctx->aux.stream) cudaStreamDestroy(ctx->aux.stream);
@@ -345,6 +413,8 @@ axr_status axr_sync(axr_context* ctx) {
         AXR_CUDA(ctx, cudaMemset(&ctx->counters->error, 0, sizeof(uint32_t)));
         if (err & kErrBarrier)
             return fail(ctx, AXR_E_TIMEOUT, "a grid barrier of the batched kernel timed out (error bits 0x%x)", err);
+        if (err & kErrTma)
+            return fail(ctx, AXR_E_TIMEOUT, "a tile load of the binned form did not arrive (error bits 0x%x)", err);
         return fail(ctx, AXR_E_CAPACITY, "device reported error bits 0x%x", err);
     }
     return AXR_OK;
@@ -354,7 +424,18 @@ axr_status axr_reserve(axr_context* ctx, uint32_t max_faces) {
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
     std::lock_guard<std::mutex> lk(ctx->mu);
     DeviceGuard g(ctx->device);
-    return grow_scratch(ctx, max_faces, max_faces * 3u, 3840ull * 2160ull);
+    axr_status st = grow_scratch(ctx, max_faces, max_faces * 3u, 3840ull * 2160ull);
+    if (st != AXR_OK) return st;
+    // the binned form's bins for a 3840x2160 framebuffer in the smallest-bin shape
+    axr_framebuffer probe{};
+    probe.tiles_x = (3840 + kTile - 1) / kTile;
+    probe.tiles_y = (2160 + kTile - 1) / kTile;
+    // at most one bin per tile; a sized-per-draw capacity is a power of two below
+    // 4 * faces / bins (at least 64), so bins * capacity stays below max(64 * bins, 4 * faces)
+    const uint32_t bins = (uint32_t)probe.tiles_x * (uint32_t)probe.tiles_y;
+    const size_t entries = ctx->bin_params.capacity > 0 ? (size_t)bins * (size_t)ctx->bin_params.capacity
+                                                        : std::max<size_t>(64ull * bins, 4ull * max_faces);
+    return grow_bins(ctx, bins, entries, std::max<uint32_t>(1u << 16, max_faces / 4));
 }
 
 void* axr_host_alloc(size_t bytes) {
@@ -868,6 +949,12 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
     if (st != AXR_OK) return st;
     DevUniforms u = make_uniforms(ctx->camera, ctx->shader, model);
     DrawParams p = make_params(ctx, mesh, ctx->fb, u);
+    BinPlan bp{};
+    if (ctx->draw_form == AXR_DRAW_BINNED) {
+        bp = plan_bins(ctx->bin_params, ctx->fb, mesh->num_drawn);
+        st = grow_bins(ctx, bp.bins(), (size_t)bp.bins() * bp.cap, bp.crec);
+        if (st != AXR_OK) return st;
+    }
     cudaEvent_t* ev = nullptr;
     if (ctx->profile && !ctx->capturing) {
         while (ctx->event_pool.size() < ctx->events_used + kStageEvents) {
@@ -878,7 +965,47 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
         ev = &ctx->event_pool[ctx->events_used];
         ctx->events_used += kStageEvents;
     }
-    AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, &ctx->aux, ev, &ctx->launches));
+    if (ctx->draw_form != AXR_DRAW_BINNED) {
+        AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, &ctx->aux, ev, &ctx->launches));
+        return AXR_OK;
+    }
+    SoloBinned sb{};
+    sb.color_map = ctx->fb->color_map;
+    sb.depth_map = ctx->fb->depth_map;
+    sb.p = p;
+    sb.p.bins = DevBins{ctx->bin_entries, 0u, bp.cap, bp.bins_x, bp.bins_y, bp.tw, bp.th,
+                        (uint16_t)ctx->bin_params.thread_pixels};
+    sb.bins = BinSet{ctx->bin_mem, reinterpret_cast<uint32_t*>(ctx->bin_mem + 1), ctx->bin_crec, bp.bins(),
+                     ctx->crec_cap};
+    sb.flags = ctx->fb->tma ? kBatchTma : 0u;
+    AXR_CUDA(ctx, launch_draw_binned(sb, ctx->stream, ev, &ctx->launches));
+    return AXR_OK;
+}
+
+axr_status axr_set_draw_form(axr_context* ctx, int32_t form) {
+    if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
+    if (form != AXR_DRAW_BINNED && form != AXR_DRAW_KEYED) return fail(ctx, AXR_E_INVALID, "unknown draw form %d", form);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->draw_form = form;
+    return AXR_OK;
+}
+
+int32_t axr_get_draw_form(const axr_context* ctx) { return ctx ? ctx->draw_form : -1; }
+
+axr_status axr_set_bin_params(axr_context* ctx, const axr_bin_params* params) {
+    if (!ctx || !params) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    if (!valid_bin_params(*params, true))
+        return fail(ctx, AXR_E_INVALID, "bin parameters: capacity %d (0 or 16..65536), shape %d x %d tiles (0, or 1, 2, "
+                    "4 or 8 each with at most 8 in all), thread pixels %d (1..2048)", params->capacity, params->tiles_x,
+                    params->tiles_y, params->thread_pixels);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->bin_params = *params;
+    return AXR_OK;
+}
+
+axr_status axr_get_bin_params(const axr_context* ctx, axr_bin_params* out) {
+    if (!ctx || !out) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    *out = ctx->bin_params;
     return AXR_OK;
 }
 

@@ -66,6 +66,23 @@ axr_status png_batch_encode_locked(axr_context* ctx, axr_png_batch* b, int32_t c
 cudaError_t png_batch_query(const axr_png_batch* b);
 void png_batch_file(const axr_png_batch* b, int32_t i, const void** dev, uint64_t* size);
 
+// Bin parameters within their documented ranges (capacity and shape 0 allowed only where
+// they mean "chosen per draw").
+inline bool valid_bin_params(const axr_bin_params& b, bool allow_auto) {
+    auto pow2_tiles = [](int32_t v) { return v == 1 || v == 2 || v == 4 || v == 8; };
+    const bool cap_ok = (allow_auto && b.capacity == 0) || (b.capacity >= 16 && b.capacity <= 65536);
+    const int32_t ty = b.tiles_y ? b.tiles_y : (b.tiles_x ? 8 / b.tiles_x : 1);
+    const bool shape_ok = (allow_auto && b.tiles_x == 0) ||
+                          (pow2_tiles(b.tiles_x) && pow2_tiles(ty) && b.tiles_x * ty <= 8);
+    return cap_ok && shape_ok && b.thread_pixels >= 1 && b.thread_pixels <= 2048;
+}
+
+// Tiles across and down of a bin from valid parameters with a fixed shape.
+inline void bin_shape(const axr_bin_params& b, uint8_t* tw, uint8_t* th) {
+    *tw = (uint8_t)b.tiles_x;
+    *th = (uint8_t)(b.tiles_y ? b.tiles_y : 8 / b.tiles_x);
+}
+
 template <class T>
 cudaError_t dmalloc(T** p, size_t count) {
     *p = nullptr;

@@ -10,6 +10,7 @@
 
 #include "axr.h"
 #include "batch_types.h"
+#include "binned.h"
 #include "device_types.h"
 #include "hostmath.h"
 #include "kernels.h"
@@ -132,6 +133,18 @@ struct axr_context {
     // batched form: per density class, the largest pixel box rasterised per thread
     // (autotuned), and the reusable plan of axr_draw_batch
     int32_t tune_small[AXR_TUNE_CLASSES] = {64, 64, 64, 64, 64, 64};
+    // binned batched form: bin parameters per density class (autotuned)
+    axr_bin_params tune_bin[AXR_TUNE_CLASSES] = {{256, 4, 64, 2}, {256, 4, 64, 2}, {256, 4, 64, 2},
+                                                 {256, 4, 64, 2}, {256, 4, 64, 2}, {256, 4, 64, 2}};
+    // binned per-draw form (axr_draw_mesh): its parameters and scratch: the bin counters
+    // followed by the bin counts, the bins' entries and the clipped-triangle records
+    int draw_form = AXR_DRAW_BINNED;
+    axr_bin_params bin_params{0, 0, 64, 0};
+    axr::BinCounters* bin_mem = nullptr;
+    uint32_t* bin_entries = nullptr;
+    float4* bin_crec = nullptr;
+    uint32_t bin_count_cap = 0, crec_cap = 0;
+    size_t bin_entry_cap = 0;
     axr_batch* oneshot = nullptr;
     axr::BatchProfile* batch_prof = nullptr;  // device-side phase timing of persistent launches
     int batch_form = axr::kFormPhased;        // launch form of batches planned next

@@ -25,6 +25,8 @@
 
 #include "batch.h"
 #include "draw_body.cuh"
+#include "tma.cuh"
+#include "unit.cuh"
 
 namespace axr {
 namespace {
@@ -111,57 +113,6 @@ __device__ void profile_exit(BatchProfile* prof) {
     for (int k = 0; k < 4; ++k) atomicAdd(&prof->phase_ns[k], t[k + 1] > t[k] ? t[k + 1] - t[k] : 0ull);
     atomicAdd(&prof->launches, 1ull);
     prof->exits = 0ull;
-}
-
-struct UnitInfo {
-    uint32_t draw;   // index into the batch
-    uint32_t local;  // unit index inside the draw
-    uint32_t flags, clear_bgra;
-    float clear_depth;
-    uint32_t pad_[3];
-};
-
-// Warp 0 copies the parameters of work unit u's draw into shared memory.
-__device__ __forceinline__ void stage_unit(const BatchParams& bp, uint32_t u, DrawParams* dst, UnitInfo* info) {
-    if (threadIdx.x < 32) {
-        const uint2 r = __ldg(reinterpret_cast<const uint2*>(bp.units) + u);
-        const BatchDraw* bd = &bp.draws[r.x];
-        const uint4* src = reinterpret_cast<const uint4*>(&bd->p);
-        uint4* out = reinterpret_cast<uint4*>(dst);
-        for (int k = (int)threadIdx.x; k < (int)(sizeof(DrawParams) / 16); k += 32) out[k] = __ldg(src + k);
-        if (threadIdx.x == 0)
-            *info = UnitInfo{r.x, r.y, __ldg(&bd->flags), __ldg(&bd->clear_bgra), __ldg(&bd->clear_depth), {0, 0, 0}};
-    }
-}
-
-// ---- TMA tensor store of a staged 16x16 tile (PTX ISA: cp.async.bulk.tensor, bulk_group)
-__device__ __forceinline__ void tma_fence_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void tma_store_tile(const TensorMap128* map, const uint32_t* smem, int x, int y) {
-    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
-                 :
-                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(s), "r"(x), "r"(y)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-
-// Wait until at most one committed group is still reading shared memory.
-__device__ __forceinline__ void tma_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
-
-__device__ __forceinline__ void tma_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-
-// Winner that came out of the clipper: its inputs from the clipper re-run, then the
-// fragment; kept out of line so that the clipper's state does not raise the register count
-// of the tile pass.
-template <int S>
-__device__ __noinline__ bool shade_clipped(const DrawParams& p, uint32_t tag, int gx, int gy, float old, uint32_t* bgra,
-                                           float* z) {
-    Screen s;
-    VSOut vo[3];
-    uint32_t material;
-    return clipped_inputs<S>(p, tag, s, vo, material) && shade_pixel<S>(p, gx, gy, material, s, vo, old, *bgra, *z);
 }
 
 // ---- the tile pass, in three steps over one 16x16 tile of draw `p`:
@@ -294,7 +245,7 @@ __device__ bool tile_finish(const DrawParams& p, const UnitInfo& ui, const Batch
         const float old = c.clear_d ? ui.clear_depth : t.depth[idx];
         uint32_t bgra = 0u;
         float z = 0.0f;
-        const bool ok = shade_clipped<S>(p, tag, gx, gy, old, &bgra, &z);
+        const bool ok = shade_clipped_px<S>(p, tag, gx, gy, old, &bgra, &z);
         tile_put(t, ui, c, stage, pix, idx, ok, bgra, z);
     }
     if (!c.full) return false;
@@ -591,7 +542,7 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
         __syncthreads();  // s_list, s_n, s_buf and s_tile are rewritten by the next round
     }
     // the staging buffers must have been read before the CTA exits
-    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    if (lane == 0) tma_wait_read_0();
 }
 
 // Clear of both planes of the phased form's fully cleared draws, in spans of kClearUnit

@@ -14,6 +14,7 @@
 #include "api_internal.h"
 #include "api_types.h"
 #include "batch.h"
+#include "binned.h"
 
 using namespace axr;
 using namespace axr_internal;
@@ -94,6 +95,14 @@ axr_status check_draws(axr_context* ctx, const axr_draw_desc* draws, int32_t cou
 
 uint32_t ceil_div(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
 
+// Bins of one draw of a binned batch.
+struct BinPlanD {
+    uint16_t bins_x = 0, bins_y = 0;
+    uint8_t tw = 8, th = 1;
+    uint32_t cap = 0;
+    uint16_t thread_px = 64;
+};
+
 // Build the batch's draw table and launch descriptions into `b`, (re)allocating its device
 // memory when it is too small. `async`: upload with cudaMemcpyAsync on the context stream
 // (the host table is copied before the call returns); otherwise synchronously.
@@ -133,7 +142,32 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     // large-triangle lists (the lists' capacity is shared out): one set's phases fill the
     // other's tails and gaps, e.g. the issue-bound large-triangle phase beside the
     // latency-bound tile pass.
-    const int nsets = (ctx->batch_form == kFormPhased && count >= (int32_t)kSplitMinDraws) ? 2 : 1;
+    const bool binned = ctx->batch_form == kFormBinned;
+    const int nsets =
+        ((ctx->batch_form == kFormPhased || binned) && count >= (int32_t)kSplitMinDraws) ? 2 : 1;
+    // binned form: each draw's bin shape and capacity from its density class; per launch set
+    // the bins (counts) and bin entries of its draws, and its clipped-triangle records
+    std::vector<BinPlanD> bplan((size_t)count);
+    uint64_t set_bins[2] = {0, 0}, set_entries[2] = {0, 0}, set_faces[2] = {0, 0};
+    if (binned) {
+        for (const auto& g : groups)
+            for (size_t k = 0; k < g.second.second - g.second.first; ++k) {
+                const int set = (int)(k % (size_t)nsets);
+                const int32_t i = order[g.second.first + k];
+                BinPlanD& bp = bplan[(size_t)i];
+                const axr_bin_params& tp = ctx->tune_bin[density_class(draws[i])];
+                bin_shape(tp, &bp.tw, &bp.th);
+                bin_geometry(draws[i].framebuffer->tiles_x, draws[i].framebuffer->tiles_y, bp.tw, bp.th, &bp.bins_x,
+                             &bp.bins_y);
+                bp.cap = (uint32_t)tp.capacity;
+                bp.thread_px = (uint16_t)tp.thread_pixels;
+                set_bins[set] += (uint64_t)bp.bins_x * bp.bins_y;
+                set_entries[set] += (uint64_t)bp.bins_x * bp.bins_y * bp.cap;
+                set_faces[set] += draws[i].mesh->num_drawn;
+            }
+    }
+    uint32_t set_crec[2];
+    for (int s = 0; s < 2; ++s) set_crec[s] = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1u << 16, set_faces[s] / 4), 1u << 24);
     const uint32_t large_cap = std::max<uint32_t>(65536, (large_cap_all + nsets - 1) / nsets);
     const uint32_t item_cap = std::max<uint32_t>(1u << 20, (item_cap_all + nsets - 1) / nsets);
     // work units of every draw (the same counts as the loop below assigns)
@@ -145,19 +179,28 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         const axr_draw_desc& d = draws[i];
         const bool drawn = d.mesh->num_drawn > 0;
         total_units += (drawn ? ceil_div(d.mesh->num_vertices, kVertUnit) : 0u) + ceil_div(d.mesh->num_drawn, kFaceUnit);
-        if (drawn || (d.clear_flags & (AXR_DRAW_CLEAR_COLOR | AXR_DRAW_CLEAR_DEPTH)))
+        if (binned)
+            total_units += (uint64_t)bplan[(size_t)i].bins_x * bplan[(size_t)i].bins_y;
+        else if (drawn || (d.clear_flags & (AXR_DRAW_CLEAR_COLOR | AXR_DRAW_CLEAR_DEPTH)))
             total_units += ceil_div((uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y, tile_unit);
         if (form == kFormPhased && (d.clear_flags & AXR_DRAW_CLEAR_COLOR) && (d.clear_flags & AXR_DRAW_CLEAR_DEPTH))
             total_units += ceil_div((uint64_t)d.framebuffer->width * d.framebuffer->height, kClearUnit);
     }
     const size_t table_bytes = align256(sizeof(BatchDraw) * (size_t)std::max(count, 1));
     const size_t units_bytes = align256(sizeof(UnitRef) * std::max<size_t>(total_units, 1));
-    const size_t set_list_bytes = align256(sizeof(LargeTri) * (size_t)large_cap) +
-                                  align256(sizeof(uint32_t) * (size_t)large_cap) +
-                                  align256(sizeof(LargeItem) * (size_t)item_cap);
+    size_t set_list_bytes = align256(sizeof(LargeTri) * (size_t)large_cap) +
+                            align256(sizeof(uint32_t) * (size_t)large_cap) +
+                            align256(sizeof(LargeItem) * (size_t)item_cap);
+    size_t set_bytes[2] = {0, 0};  // binned: counters + counts, entries, clipped records
+    if (binned) {
+        set_list_bytes = 0;
+        for (int s = 0; s < nsets; ++s)
+            set_bytes[s] = align256(sizeof(BinCounters) + sizeof(uint32_t) * set_bins[s]) +
+                           align256(sizeof(uint32_t) * set_entries[s]) + align256(16 * (size_t)kRasterRec * set_crec[s]);
+    }
     const size_t counter_bytes = align256(sizeof(DevCounters));
     const size_t need = table_bytes + units_bytes + align256(cache_bytes) + set_list_bytes * nsets +
-                        counter_bytes * (nsets - 1);
+                        counter_bytes * (nsets - 1) + set_bytes[0] + set_bytes[1];
     if (need > b->bytes) {
         if (ctx->capturing) return fail(ctx, AXR_E_CAPACITY, "a batch cannot be planned during graph capture");
         AXR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -186,6 +229,21 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
         // statistics and error bits start at zero; the merge after each launch zeroes them again
         AXR_CUDA(ctx, cudaMemsetAsync(d_counters[1], 0, sizeof(DevCounters), ctx->stream));
     }
+    BinCounters* d_bin_counters[2] = {nullptr, nullptr};
+    uint32_t* d_bin_entries[2] = {nullptr, nullptr};
+    float4* d_crec[2] = {nullptr, nullptr};
+    if (binned) {
+        unsigned char* q = lists + set_list_bytes * (size_t)nsets + counter_bytes * (size_t)(nsets - 1);
+        for (int s = 0; s < nsets; ++s) {
+            d_bin_counters[s] = reinterpret_cast<BinCounters*>(q);
+            q += align256(sizeof(BinCounters) + sizeof(uint32_t) * set_bins[s]);
+            d_bin_entries[s] = reinterpret_cast<uint32_t*>(q);
+            q += align256(sizeof(uint32_t) * set_entries[s]);
+            d_crec[s] = reinterpret_cast<float4*>(q);
+            q += align256(16 * (size_t)kRasterRec * set_crec[s]);
+        }
+    }
+    uint64_t set_bin_at[2] = {0, 0}, set_entry_at[2] = {0, 0};  // binned: next bin / entry of each set
 
     std::vector<BatchDraw> table((size_t)std::max(count, 1));
     std::vector<UnitRef> units;
@@ -194,6 +252,7 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
     for (const auto& g : groups) {
         const size_t first = g.second.first, last = g.second.second, n = last - first;
         std::vector<UnitRef> set_uv[2], set_uf[2], set_ut[2], set_uc[2];
+        const uint64_t group_bin_at[2] = {set_bin_at[0], set_bin_at[1]};  // the launches' first bins
         for (size_t k = 0; k < n; ++k) {
             const int set = (int)(k % (size_t)nsets);
             std::vector<UnitRef>&uv = set_uv[set], &uf = set_uf[set], &ut = set_ut[set], &uc = set_uc[set];
@@ -216,10 +275,20 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             cache += align256(16 * (size_t)m->num_vertices * (size_t)vattr_float4s(d.shader.kind));
             float4* rec = reinterpret_cast<float4*>(cache);
             cache += align256(16 * (size_t)kRecFloat4 * m->num_drawn);
-            p.scratch = DevScratch{d_counters[set], d_large[set], d_items[set], vscreen, vattr, nullptr, nullptr,
-                                   large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw[set], rec};
+            p.scratch = binned ? DevScratch{d_counters[set], nullptr, nullptr, vscreen, vattr, nullptr, nullptr, 0u, 0u,
+                                            m->num_vertices, 0u, 0, 0, nullptr, rec}
+                               : DevScratch{d_counters[set], d_large[set], d_items[set], vscreen, vattr, nullptr, nullptr,
+                                            large_cap, item_cap, m->num_vertices, 0u, 0, 0, d_large_draw[set], rec};
             p.small_max_pixels = ctx->tune_small[density_class(d)];
             p.draw = (uint32_t)k;
+            if (binned) {
+                const BinPlanD& bp = bplan[(size_t)order[first + k]];
+                const uint32_t nb = (uint32_t)bp.bins_x * bp.bins_y;
+                p.bins = DevBins{d_bin_entries[set] + set_entry_at[set], (uint32_t)(set_bin_at[set] - group_bin_at[set]),
+                                 bp.cap, bp.bins_x, bp.bins_y, bp.tw, bp.th, bp.thread_px};
+                set_bin_at[set] += nb;
+                set_entry_at[set] += (uint64_t)nb * bp.cap;
+            }
             bd.flags = (d.clear_flags & AXR_DRAW_CLEAR_COLOR ? kBatchClearColor : 0u) |
                        (d.clear_flags & AXR_DRAW_CLEAR_DEPTH ? kBatchClearDepth : 0u) | (fb->tma ? kBatchTma : 0u);
             // bytes B, G, R, A (src/framebuffer.cpp:26-36)
@@ -229,7 +298,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             const bool drawn = m->num_drawn > 0;
             const uint32_t nv = drawn ? ceil_div(m->num_vertices, kVertUnit) : 0u;
             const uint32_t nf = ceil_div(m->num_drawn, kFaceUnit);
-            const uint32_t nt = (drawn || bd.flags & (kBatchClearColor | kBatchClearDepth))
+            const uint32_t nt = binned ? (uint32_t)p.bins.bins_x * p.bins.bins_y
+                                : (drawn || bd.flags & (kBatchClearColor | kBatchClearDepth))
                                     ? ceil_div((uint64_t)fb->tiles_x * fb->tiles_y, tile_unit)
                                     : 0u;
             for (uint32_t j = 0; j < nv; ++j) uv.push_back(UnitRef{(uint32_t)k, j});
@@ -268,6 +338,10 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             bp.large_cap = large_cap;
             bp.item_cap = item_cap;
             bp.tiles_per_warp = tiles_per_warp;
+            if (binned)
+                bp.bins = BinSet{d_bin_counters[set],
+                                 reinterpret_cast<uint32_t*>(d_bin_counters[set] + 1) + group_bin_at[set], d_crec[set],
+                                 (uint32_t)(set_bin_at[set] - group_bin_at[set]), set_crec[set]};
             if (bp.vert_units + bp.face_units + bp.tile_units > 0) b->launches.push_back(L);
         }
     }
@@ -325,7 +399,7 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
         bp.collect_stats = ctx->collect_stats;
         bp.prof = ctx->profile && b->form == kFormPersistent ? ctx->batch_prof : nullptr;
         cudaEvent_t* ev = nullptr;
-        if (ctx->profile && b->form == kFormPhased && !ctx->capturing) {
+        if (ctx->profile && b->form != kFormPersistent && !ctx->capturing) {
             while (ctx->batch_events.size() < ctx->batch_events_used + 6) {
                 cudaEvent_t e;
                 AXR_CUDA(ctx, cudaEventCreate(&e));
@@ -337,8 +411,11 @@ axr_status launch_planned(axr_context* ctx, const axr_batch* b) {
         // set 1 clears right before its tile pass: its clear (bound by the write rate) then
         // meets set 0's latency-bound tile pass, and set 0's clear meets set 1's vertex and
         // face phases, instead of the two clears meeting each other
-        AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, L.set ? side : ctx->stream, ev,
-                                   &ctx->launches, split && L.set > 0));
+        if (b->form == kFormBinned)
+            AXR_CUDA(ctx, launch_batch_binned(L.shader, bp, L.set ? side : ctx->stream, ev, &ctx->launches));
+        else
+            AXR_CUDA(ctx, launch_batch(L.shader, bp, b->form, ctx->cfg.num_sms, L.set ? side : ctx->stream, ev,
+                                       &ctx->launches, split && L.set > 0));
     }
     if (b->sets > 1) {
         // set 1's statistics and error bits into the context's counters, which axr_sync and
@@ -510,6 +587,24 @@ axr_status axr_batch_set_tuning(axr_context* ctx, const int32_t small_max_pixels
     return AXR_OK;
 }
 
+axr_status axr_batch_get_bin_tuning(const axr_context* ctx, axr_bin_params out[AXR_TUNE_CLASSES]) {
+    if (!ctx || !out) return fail(nullptr, AXR_E_INVALID, "NULL argument");
+    std::memcpy(out, ctx->tune_bin, sizeof(ctx->tune_bin));
+    return AXR_OK;
+}
+
+axr_status axr_batch_set_bin_tuning(axr_context* ctx, const axr_bin_params params[AXR_TUNE_CLASSES]) {
+    if (!ctx || !params) return fail(ctx, AXR_E_INVALID, "NULL argument");
+    for (int k = 0; k < AXR_TUNE_CLASSES; ++k)
+        if (!valid_bin_params(params[k], false))
+            return fail(ctx, AXR_E_INVALID, "class %d: bin parameters (capacity %d: 16..65536, shape %d x %d tiles: 1, "
+                        "2, 4 or 8 each with at most 8 in all, thread pixels %d: 1..2048)", k, params[k].capacity,
+                        params[k].tiles_x, params[k].tiles_y, params[k].thread_pixels);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::memcpy(ctx->tune_bin, params, sizeof(ctx->tune_bin));
+    return AXR_OK;
+}
+
 axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int32_t count, int32_t repeats,
                               int32_t out_small_max_pixels[AXR_TUNE_CLASSES]) {
     NvtxRange nvtx_range("axr_batch_autotune");
@@ -541,11 +636,57 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
         if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
         return e == cudaSuccess ? AXR_OK : cuda_fail(ctx, e, "autotune timing");
     };
-    // launch form: both forms on the whole batch
+    // the binned form's bin parameters per density class, by coordinate descent on the
+    // sub-batch of that class: per-thread raster limit, then bin shape, then capacity
     {
+        const int saved_form = ctx->batch_form;
+        ctx->batch_form = kFormBinned;
+        static const int32_t kThreadPx[] = {16, 32, 64, 128, 256};
+        static const int32_t kShapes[][2] = {{8, 1}, {4, 2}, {2, 4}, {4, 1}, {2, 2}, {2, 1}, {1, 1}};
+        static const int32_t kCapacity[] = {64, 128, 256, 512, 1024, 2048};
+        for (int k = 0; k < AXR_TUNE_CLASSES && st == AXR_OK; ++k) {
+            const std::vector<axr_draw_desc>& sub = by_class[(size_t)k];
+            if (sub.empty()) continue;
+            auto descend = [&](int32_t axr_bin_params::*field, const int32_t* cands, size_t n) {
+                float best_ms = 0.f;
+                int32_t best = ctx->tune_bin[k].*field;
+                for (size_t c = 0; c < n && st == AXR_OK; ++c) {
+                    ctx->tune_bin[k].*field = cands[c];
+                    float ms = 0.f;
+                    if ((st = time_plan(sub.data(), (int32_t)sub.size(), &ms)) != AXR_OK) break;
+                    if (best_ms == 0.f || ms < best_ms) {
+                        best_ms = ms;
+                        best = cands[c];
+                    }
+                }
+                ctx->tune_bin[k].*field = best;
+            };
+            descend(&axr_bin_params::thread_pixels, kThreadPx, sizeof(kThreadPx) / sizeof(kThreadPx[0]));
+            {  // bin shape: tiles across and down together
+                float best_ms = 0.f;
+                axr_bin_params best = ctx->tune_bin[k];
+                for (const auto& sh : kShapes) {
+                    if (st != AXR_OK) break;
+                    ctx->tune_bin[k].tiles_x = sh[0];
+                    ctx->tune_bin[k].tiles_y = sh[1];
+                    float ms = 0.f;
+                    if ((st = time_plan(sub.data(), (int32_t)sub.size(), &ms)) != AXR_OK) break;
+                    if (best_ms == 0.f || ms < best_ms) {
+                        best_ms = ms;
+                        best = ctx->tune_bin[k];
+                    }
+                }
+                ctx->tune_bin[k] = best;
+            }
+            descend(&axr_bin_params::capacity, kCapacity, sizeof(kCapacity) / sizeof(kCapacity[0]));
+        }
+        ctx->batch_form = saved_form;
+    }
+    // launch form: the three forms on the whole batch
+    if (st == AXR_OK) {
         float best_ms = 0.f;
         int best = ctx->batch_form;
-        for (int form : {kFormPersistent, kFormPhased}) {
+        for (int form : {kFormPersistent, kFormPhased, kFormBinned}) {
             ctx->batch_form = form;
             float ms = 0.f;
             if ((st = time_plan(draws, count, &ms)) != AXR_OK) break;
@@ -556,7 +697,8 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
         }
         ctx->batch_form = best;
     }
-    for (int k = 0; k < AXR_TUNE_CLASSES && st == AXR_OK; ++k) {
+    // the keyed forms' per-thread pixel-box limit per density class
+    for (int k = 0; k < AXR_TUNE_CLASSES && st == AXR_OK && ctx->batch_form != kFormBinned; ++k) {
         const std::vector<axr_draw_desc>& sub = by_class[(size_t)k];
         if (sub.empty()) continue;
         float best_ms = 0.f;
@@ -584,7 +726,7 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
 
 axr_status axr_batch_set_form(axr_context* ctx, int32_t form) {
     if (!ctx) return fail(nullptr, AXR_E_INVALID, "context is NULL");
-    if (form != AXR_BATCH_PERSISTENT && form != AXR_BATCH_PHASED)
+    if (form != AXR_BATCH_PERSISTENT && form != AXR_BATCH_PHASED && form != AXR_BATCH_BINNED)
         return fail(ctx, AXR_E_INVALID, "unknown batch launch form %d", form);
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->batch_form = form;

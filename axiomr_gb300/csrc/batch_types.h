@@ -79,13 +79,18 @@ struct BatchParams {
     uint32_t large_cap, item_cap;
     int32_t collect_stats;
     uint32_t tiles_per_warp;      // tiles a warp takes per tile unit (unit = 8 warps x this)
+    BinSet bins;                  // binned form: the launch set's bin counts and clipped records
 };
 
 // Launch forms of a batch (chosen per batch by the autotuner):
 //   kFormPersistent  one cooperative launch: the four phases behind grid barriers
 //   kFormPhased      four launches (one per phase), each over the work units of all draws
+//   kFormBinned      three launches over the work units of all draws: vertices, faces
+//                    (setup and binning), bins (raster, shading and write-out in shared
+//                    memory); tile units are bins of 8 tiles, one CTA each
 constexpr int kFormPersistent = 0;
 constexpr int kFormPhased = 1;
+constexpr int kFormBinned = 2;
 constexpr uint32_t kPersistentTilesPerWarp = 8;
 constexpr uint32_t kPhasedTilesPerWarp = 4;
 constexpr uint32_t kSplitMinDraws = 128;  // phased batches of this many draws run as two launch sets

@@ -131,6 +131,7 @@ constexpr unsigned kCountersReset = 5 * sizeof(uint32_t);
 constexpr unsigned kBatchCountersReset = 7 * sizeof(uint32_t);  // + the grid-barrier words
 constexpr uint32_t kErrOrdinal = 1u;  // more faces than a depth key can order
 constexpr uint32_t kErrIndex = 2u;    // a face indexes a vertex beyond the mesh (face skipped)
+constexpr uint32_t kErrTma = 8u;      // a tile load of the binned form did not arrive in time
 
 // Per-vertex cache written by the vertex pass of each draw:
 //   vscreen[i] = (screen x, screen y, NDC z, clip-plane masks as uint bits)
@@ -158,9 +159,55 @@ struct DevScratch {
 
 // Shading record of an unclipped triangle that can win a pixel, written by the geometry
 // step at its draw-order position and read by the shading step in place of re-deriving the
-// setup from the face: edge terms, 1/area, vertex depths, x_lo (the row-start rule of
-// eval_pixel), material and the three vertex indices (for the cached vertex outputs).
+// setup from the face: the raster record (edge terms, 1/area, vertex depths, pixel range,
+// material; x_lo gives the row-start rule of eval_pixel) and the three vertex indices (for
+// the cached vertex outputs).
 constexpr int kRecFloat4 = 5;
+
+// Binned form: the framebuffer is cut into bins of 8 tiles of 16x16 (tw x th tiles: 8x1,
+// 4x2 or 2x4). The face kernel appends each set-up triangle to the entry list of every bin
+// its pixel box reaches (less the bins its edges provably miss); the tile kernel then
+// rasterises one bin's list into depth keys in shared memory, shades the winners and
+// writes the bin's colour and depth once. An entry is a draw-order position (the
+// triangle's raster record is rec[position]) or kClipEntry | k for a clipped triangle
+// (record k of the launch set's clipped-record list).
+constexpr int kBinTiles = 8;
+constexpr uint32_t kClipEntry = 0x80000000u;
+
+struct DevBins {
+    uint32_t* entries;    // this draw's bins, `cap` entries each (row-major bins)
+    uint32_t base;        // index of this draw's bin 0 in the launch set's bin counts
+    uint32_t cap;         // entries per bin; a bin offered more spills the rest (see BinSet)
+    uint16_t bins_x, bins_y;
+    uint8_t tw, th;       // tiles per bin across and down (tw * th == kBinTiles)
+    uint16_t thread_px;   // triangle-in-bin rectangles of at most this many pixels are
+                          // rasterised by one thread; larger ones by a whole warp
+};
+
+// Per launch set (or per context for single draws): zeroed before every launch together
+// with the bin counts that follow it in memory.
+struct BinCounters {
+    uint32_t crec_count;  // clipped-triangle records reserved (may exceed the capacity)
+    uint32_t spill;       // (triangle, bin) pairs that found their bin (or the clipped
+                          // records) full and went to the framebuffer's key plane instead
+    uint32_t pad_[14];
+};
+static_assert(sizeof(BinCounters) == 64, "bin counts start 64 bytes after the counters");
+
+struct BinSet {
+    BinCounters* counters;
+    uint32_t* count;      // per bin of the set: entries offered (may exceed the bin's cap)
+    float4* crec;         // clipped-triangle raster records, kRasterRec float4 each
+    uint32_t nbins;
+    uint32_t crec_cap;
+};
+
+// Raster record of a set-up triangle (64 bytes): edge a, b, c of edges 0..2 after the
+// area-sign flip, 1/area, vertex depths, the covered pixel range [x_lo, x_hi) x [y_lo, y_hi)
+// packed as 16-bit pairs, and one word: the material (a shading record at the triangle's
+// draw-order position, which adds a fifth float4 with the three vertex indices) or the
+// depth-key tag (a clipped triangle's record).
+constexpr int kRasterRec = 4;
 
 struct alignas(16) DrawParams {
     DevMesh mesh;
@@ -169,6 +216,8 @@ struct alignas(16) DrawParams {
     DevScratch scratch;
     int32_t small_max_pixels;  // triangles whose pixel box is at most this are rasterised per thread
     uint32_t draw;             // index of the draw in its batch (0 for a single draw)
+    DevBins bins;              // binned form only
+    uint32_t pad_[2];
 };
 
 }  // namespace axr

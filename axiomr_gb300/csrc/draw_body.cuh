@@ -119,14 +119,34 @@ __device__ __forceinline__ void load_large(const LargeTri* src, Edges& e, uint32
     e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
 }
 
-__device__ __forceinline__ void store_record(const DrawParams& p, uint32_t ordinal, const Edges& e, uint32_t material,
-                                             const uint3& f) {
-    float4* r = p.scratch.rec + (size_t)kRecFloat4 * ordinal;
+// Raster record (kRasterRec float4, see device_types.h): edges, 1/area, depths, pixel range
+// and one extra word (material or tag).
+__device__ __forceinline__ void store_raster(float4* r, const Edges& e, uint32_t word) {
     r[0] = make_float4(e.a[0], e.b[0], e.c[0], e.a[1]);
     r[1] = make_float4(e.b[1], e.c[1], e.a[2], e.b[2]);
     r[2] = make_float4(e.c[2], e.inv_area, e.z[0], e.z[1]);
-    r[3] = make_float4(e.z[2], __int_as_float(e.x_lo), __uint_as_float(material), __uint_as_float(f.x));
-    r[4] = make_float4(__uint_as_float(f.y), __uint_as_float(f.z), 0.0f, 0.0f);
+    const uint32_t xs = (uint32_t)e.x_lo | ((uint32_t)e.x_hi << 16);
+    const uint32_t ys = (uint32_t)e.y_lo | ((uint32_t)e.y_hi << 16);
+    r[3] = make_float4(e.z[2], __uint_as_float(xs), __uint_as_float(ys), __uint_as_float(word));
+}
+
+__device__ __forceinline__ uint32_t unpack_raster(const float4 r0, const float4 r1, const float4 r2, const float4 r3,
+                                                  Edges& e) {
+    e.a[0] = r0.x; e.b[0] = r0.y; e.c[0] = r0.z; e.a[1] = r0.w;
+    e.b[1] = r1.x; e.c[1] = r1.y; e.a[2] = r1.z; e.b[2] = r1.w;
+    e.c[2] = r2.x; e.inv_area = r2.y; e.z[0] = r2.z; e.z[1] = r2.w;
+    e.z[2] = r3.x;
+    const uint32_t xs = __float_as_uint(r3.y), ys = __float_as_uint(r3.z);
+    e.x_lo = (int)(xs & 0xFFFFu); e.x_hi = (int)(xs >> 16);
+    e.y_lo = (int)(ys & 0xFFFFu); e.y_hi = (int)(ys >> 16);
+    return __float_as_uint(r3.w);
+}
+
+__device__ __forceinline__ void store_record(const DrawParams& p, uint32_t ordinal, const Edges& e, uint32_t material,
+                                             const uint3& f) {
+    float4* r = p.scratch.rec + (size_t)kRecFloat4 * ordinal;
+    store_raster(r, e, material);
+    r[4] = make_float4(__uint_as_float(f.x), __uint_as_float(f.y), __uint_as_float(f.z), 0.0f);
 }
 
 // kCoherent: the record was written earlier in the same launch (plain loads).
@@ -135,13 +155,9 @@ __device__ __forceinline__ uint32_t load_record(const DrawParams& p, uint32_t or
     const float4* r = p.scratch.rec + (size_t)kRecFloat4 * ordinal;
     const float4 r0 = ld_cached<kCoherent>(r), r1 = ld_cached<kCoherent>(r + 1), r2 = ld_cached<kCoherent>(r + 2);
     const float4 r3 = ld_cached<kCoherent>(r + 3), r4 = ld_cached<kCoherent>(r + 4);
-    e.a[0] = r0.x; e.b[0] = r0.y; e.c[0] = r0.z; e.a[1] = r0.w;
-    e.b[1] = r1.x; e.c[1] = r1.y; e.a[2] = r1.z; e.b[2] = r1.w;
-    e.c[2] = r2.x; e.inv_area = r2.y; e.z[0] = r2.z; e.z[1] = r2.w;
-    e.z[2] = r3.x;
-    e.x_lo = __float_as_int(r3.y);
-    f = make_uint3(__float_as_uint(r3.w), __float_as_uint(r4.x), __float_as_uint(r4.y));
-    return __float_as_uint(r3.z);
+    const uint32_t material = unpack_raster(r0, r1, r2, r3, e);
+    f = make_uint3(__float_as_uint(r4.x), __float_as_uint(r4.y), __float_as_uint(r4.z));
+    return material;
 }
 
 // One triangle that survived clipping: cull, set up, then rasterise it here or queue its
@@ -506,6 +522,18 @@ __device__ __forceinline__ bool shade_unclipped(const DrawParams& p, uint32_t ta
     bgra = pack_bgra(col);
     z = r.z;
     return true;
+}
+
+// Winner that came out of the clipper: its inputs from the clipper re-run, then the
+// fragment; kept out of line so that the clipper's state does not raise the register count
+// of the shading loops that call it.
+template <int S>
+__device__ __noinline__ bool shade_clipped_px(const DrawParams& p, uint32_t tag, int px, int py, float old_depth,
+                                              uint32_t* bgra, float* z) {
+    Screen s;
+    VSOut vo[3];
+    uint32_t material;
+    return clipped_inputs<S>(p, tag, s, vo, material) && shade_pixel<S>(p, px, py, material, s, vo, old_depth, *bgra, *z);
 }
 
 }  // namespace

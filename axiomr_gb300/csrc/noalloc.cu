@@ -18,15 +18,23 @@
 //
 // Set-up: the first call on each device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current; make that first call before any
-// stream capture. All calls share the array and it keeps the last call's contents: each
-// call clears the work counters it needs at zero, and two calls whose work overlaps on
-// the GPU (different streams or contexts) race on the array.
+// stream capture. The address is kept for the life of the process: after a
+// cudaDeviceReset the library's module is loaded anew and the kept address is stale, so
+// this entry point must not be used after one. All calls share the array and it keeps the
+// last call's contents: each call clears the work counters it needs at zero, and two
+// calls whose work overlaps on the GPU (different streams or contexts) race on the array.
+//
+// Reporting: after the draw, a one-thread kernel adds the array's error bits and (with
+// statistics enabled on the context) its statistics to the context's counters, so
+// axr_sync and axr_stats_read see this draw like any other; stage profiles
+// (axr_profile_read) do not include it.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
 #include "api_internal.h"
 #include "api_types.h"
+#include "batch.h"
 
 namespace {
 
@@ -111,11 +119,14 @@ extern "C" axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* me
                                reinterpret_cast<uint2*>(base + kOffShade),
                                reinterpret_cast<uint2*>(base + kOffClip),
                                kNoAllocMaxFaces, kNoAllocMaxItems, kNoAllocMaxVertices, kNoAllocMaxPixels,
-                               0, 0, nullptr, reinterpret_cast<float4*>(base + kOffRec)};
+                               ctx->collect_stats, 0, nullptr, reinterpret_cast<float4*>(base + kOffRec)};
         p.small_max_pixels = ctx->small_max_pixels;
         // the array keeps the previous call's contents: start from zeroed counters
         e = cudaMemsetAsync(counters, 0, sizeof(DevCounters), ctx->stream);
         if (e == cudaSuccess) e = launch_draw(p, ctx->cfg, ctx->stream, &ctx->aux, nullptr, &ctx->launches);
+        // the array's error bits and statistics into the context's counters
+        if (e == cudaSuccess) e = launch_merge_counters(ctx->counters, counters, ctx->stream);
+        if (e == cudaSuccess) ctx->launches += 1;
     }
     if (prev >= 0 && prev != ctx->device) cudaSetDevice(prev);
     if (e != cudaSuccess) return noalloc_fail(ctx, AXR_E_CUDA, std::string("axr_draw_mesh_noalloc: ") + cudaGetErrorString(e));

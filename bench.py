@@ -74,6 +74,10 @@ def parse_args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch")
     ap.add_argument("--no-autotune", action="store_true", help="batch: plan with the default tuning table")
+    ap.add_argument("--form", choices=("auto", "persistent", "phased", "binned"), default="auto",
+                    help="batch: launch form (auto: the autotuner's choice)")
+    ap.add_argument("--draw-form", choices=("binned", "keyed"), default="binned",
+                    help="single-draw workloads: form of the per-draw path")
     ap.add_argument("--draws", type=int, default=512, help="batch: number of draws (a smaller batch for profiling)")
     ap.add_argument("--scale", type=float, default=1.0, help="batch: framebuffer size scale (profiling)")
     ap.add_argument("--rates", default="100,500,2000,5000", help="serve: offered loads, requests/s")
@@ -282,6 +286,7 @@ def run_ours(args, dist: Dist):
     dev = dist.local_rank
     torch.cuda.set_device(dev)
     ctx = api.Context(dev)
+    ctx.draw_form = api.DRAW_KEYED if args.draw_form == "keyed" else api.DRAW_BINNED
     lib = ctx.lib
     fb = api.Framebuffer(ctx, scene.width, scene.height)
     textures = {}
@@ -429,6 +434,16 @@ def run_ours(args, dist: Dist):
     }
     kernel_names = {k: k + "_kernel" for k in stages}
     kernel_names["clipped"] = "resolve_clipped_kernel"
+    if args.draw_form == "binned":
+        # three kernels: vertices, faces (setup and binning; the profile's geometry stage) and
+        # bins (raster, shading and tile write-out; its shading stage). Algorithmic bytes: the
+        # vertex attributes, the indices, and one colour + depth write per pixel plus
+        # min(texture, 4 per shaded fragment), each where it moves
+        tex_bytes = sum(int(t.nbytes) for t in images.values())
+        algo_bytes = {"vertex": float(V) * vin, "geometry": 12.0 * F, "large": 0.0, "scan": 0.0,
+                      "shade": 8.0 * P + min(tex_bytes, 4.0 * st["shaded"]), "clipped": 0.0}
+        kernel_names = {"vertex": "solo_vertex_kernel", "geometry": "solo_face_kernel", "large": "-", "scan": "-",
+                        "shade": "solo_bin_kernel", "clipped": "-"}
     dom = max(stage_us, key=stage_us.get)
     hbm_peak, peak_kind = measured_peaks()
     achieved = algo_bytes[dom] / (stage_us[dom] * 1e-6) / 1e9
@@ -443,7 +458,8 @@ def run_ours(args, dist: Dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
-        "config": {"workload": f"{args.workload}: {desc}", "form": "plain (one drawMesh per frame)",
+        "config": {"workload": f"{args.workload}: {desc}",
+                   "form": f"plain (one drawMesh per frame, {args.draw_form} form)",
                    "l2": "flushed before every timed step (256 MiB write, outside the events)",
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU"},
         "gfrag_per_s": round(frags * value / 1e9, 3),
@@ -501,6 +517,26 @@ def batch_algo_bytes(scenes, frags: float) -> float:
         tex = sum(int(t.nbytes) for m in sc.mesh.materials for t in (m.diffuse,) if t is not None)
         b += 32.0 * V + 12.0 * F + 8.0 * sc.width * sc.height + min(tex, 4.0 * frags * F / max(1, total_faces))
     return b
+
+
+def binned_phase_bytes(scenes, shaded: float) -> dict:
+    """Algorithmic bytes of each phase of one step in the binned form, SURVEY-style frame
+    bytes split by the phase that moves them: the vertex attributes read (32 per vertex:
+    position, normal, uv) by the vertex phase, the indices (12 per face) by the face phase,
+    and one colour + one depth write per pixel (8) plus min(texture bytes, 4 per shaded
+    fragment) by the bin pass. Their sum is the frame roofline's bytes; the intermediate
+    data of the design (vertex cache, raster records, bin entries) is not counted, so the
+    measured traffic against these figures shows its cost."""
+    total_faces = sum(int(sc.mesh.indices.shape[0]) for sc in scenes)
+    v = f = px = tex = 0.0
+    for sc in scenes:
+        V, F = sc.mesh.positions.shape[0], sc.mesh.indices.shape[0]
+        t = sum(int(m.diffuse.nbytes) for m in sc.mesh.materials if m.diffuse is not None)
+        v += V
+        f += F
+        px += sc.width * sc.height
+        tex += min(t, 4.0 * shaded * F / max(1, total_faces))
+    return {"clear": 0.0, "vertex": 32.0 * v, "face": 12.0 * f, "large": 0.0, "tile": 8.0 * px + tex}
 
 
 def batch_phase_bytes(scenes, frags: float, tiles: int, dirty: int, clear_apart: bool) -> dict:
@@ -626,6 +662,9 @@ def run_batch(args, dist: Dist):
 
     # ---- autotune the per-class raster parameter on this batch, then plan it
     tuning = ctx.tuning() if args.no_autotune else api.autotune(ctx, draws, repeats=2)
+    if args.form != "auto":
+        ctx.batch_form = {"persistent": api.BATCH_PERSISTENT, "phased": api.BATCH_PHASED,
+                          "binned": api.BATCH_BINNED}[args.form]
     batch = api.Batch(ctx, draws)
     info = batch.info()
     k0 = ctx.profile()["kernel_launches"]
@@ -799,9 +838,12 @@ def run_batch(args, dist: Dist):
     alu_tflops = alu_flop / (ms * 1e-3) / 1e12
     achieved = algo / (ms * 1e-3) / 1e9
     faces = info["faces"]
-    pb = batch_phase_bytes(scenes, frags, int(info["tiles"]), int(st["tiles"]), info["form"] == 1)
+    pb = binned_phase_bytes(scenes, float(st["shaded"])) if info["form"] == 2 else \
+        batch_phase_bytes(scenes, frags, int(info["tiles"]), int(st["tiles"]), info["form"] == 1)
     dom = max(phase_ms, key=phase_ms.get)
-    kernel_of = {"clear": "batch_clear_kernel", "vertex": "batch_vertex_kernel", "face": "batch_face_kernel",
+    kernel_of = {"clear": "-", "vertex": "batch_bin_vertex_kernel", "face": "batch_bin_face_kernel", "large": "-",
+                 "tile": "batch_bin_kernel"} if info["form"] == 2 else \
+        {"clear": "batch_clear_kernel", "vertex": "batch_vertex_kernel", "face": "batch_face_kernel",
                  "large": "batch_large_kernel", "tile": "batch_tile_kernel"} if info["form"] == 1 else \
         {k: "batch_kernel" for k in phase_ms}
     dom_achieved = pb[dom] / (phase_ms[dom] * 1e-3) / 1e9 if phase_ms[dom] > 0 else 0.0
@@ -811,7 +853,12 @@ def run_batch(args, dist: Dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators in axiomr_gb300/workloads.py)",
         "config": batch_config(args, dist, n),
-        "form_desc": ("batched, phased: a clear kernel and four phase launches over the work units of "
+        "form_desc": ("batched, binned: three launches over the work units of all draws (vertices; faces, "
+                      "set up and binned into bins of 8 tiles; one CTA per bin rasterising it in shared memory, "
+                      "shading the winners and writing colour and depth once with TMA stores, clears fused)"
+                      + (", as two launch sets of alternating draws on two streams" if info["launches"] > 1 else "")
+                      if info["form"] == 2 else
+                      "batched, phased: a clear kernel and four phase launches over the work units of "
                       "all draws, as two launch sets of alternating draws on two streams"
                       if info["form"] == 1 and info["launches"] > 1 else
                       "batched, phased: a clear kernel and four phase launches per step over the work "
@@ -819,6 +866,7 @@ def run_batch(args, dist: Dist):
                       "batched, persistent: one cooperative launch per step (clears fused into the tile pass)")
         + ", replayed from a CUDA graph",
         "tuning_small_max_pixels": tuning,
+        "tuning_bins": ctx.bin_tuning(),
         "gfrag_per_s": round(frags * value / n / 1e9, 3),
         "mtri_per_s": round(faces * value / n / 1e6, 2),
         "fragments_per_step": int(frags), "shaded_per_step": int(st["shaded"]), "tested_per_step": int(st["tested"]),
@@ -871,7 +919,7 @@ def run_batch(args, dist: Dist):
                                    "definition": f"{K_BLINN_PHONG} FP32 ops per shaded fragment (Blinn-Phong "
                                                  "functor) + 9 per tested pixel; peak measured with FMA chains "
                                                  "(axr_measure_fp32_peak)"}},
-        "form": "phased" if info["form"] == 1 else "persistent",
+        "form": {0: "persistent", 1: "phased", 2: "binned"}[info["form"]],
         "clocks": sampler.summary(),
     }
     graph.close()

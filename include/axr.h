@@ -27,7 +27,7 @@ extern "C" {
 
 /* Raised whenever a struct or signature of this header changes; a program built against
  * this header can compare it with axr_abi_version() of the library it loaded. */
-#define AXR_ABI_VERSION 3
+#define AXR_ABI_VERSION 4
 int32_t axr_abi_version(void);
 
 /* The reference reports failures with exceptions or silently (src/tiled_pipeline.cpp:146,
@@ -300,6 +300,38 @@ axr_status axr_set_framebuffer(axr_context* ctx, axr_framebuffer* fb);
  * framebuffer set does nothing (src/tiled_pipeline.cpp:146). */
 axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
 
+/* Forms of axr_draw_mesh; no counterpart in the reference, both give its frame.
+ * BINNED (the default): the reference's binTrianglesToTiles / processTile /
+ * mergeTileResults (src/tiled_pipeline.cpp:368-425, 1125-1181) on the GPU. A face kernel
+ * sets up every triangle and appends it to the entry list of each bin of 8 tiles (16x16)
+ * that its box reaches; one CTA per bin then rasterises the bin's list into depth keys in
+ * shared memory, shades the winners and merges them into the framebuffer, whose tiles it
+ * loads and stores with TMA tensor copies. KEYED: the visibility of every covered pixel
+ * is decided by a 64-bit atomicMin of (depth, draw order) into the framebuffer's key
+ * plane in device memory, then a per-pixel pass shades the winners. */
+#define AXR_DRAW_BINNED 0
+#define AXR_DRAW_KEYED 1
+axr_status axr_set_draw_form(axr_context* ctx, int32_t form);
+int32_t axr_get_draw_form(const axr_context* ctx);
+
+/* Bin parameters of the binned forms: for axr_draw_mesh (axr_set_bin_params) and per
+ * density class of a batch (axr_batch_set_bin_tuning). No counterpart in the reference,
+ * whose tile size and worker batch are compile-time constants (TILE_SIZE, BATCH_SIZE,
+ * include/tiled_pipeline.hpp:28-31). A bin offered more entries than its capacity
+ * rasterises the rest through the framebuffer's key plane (slower, same result). */
+typedef struct axr_bin_params {
+    int32_t capacity;       /* entries per bin (16..65536); 0 with axr_set_bin_params: sized
+                             * per draw from its faces and framebuffer */
+    int32_t tiles_x;        /* bin shape: tiles across (1, 2, 4 or 8); 0 with
+                             * axr_set_bin_params: chosen per draw from the framebuffer size */
+    int32_t thread_pixels;  /* a triangle's part of a bin of at most this many pixels is
+                             * rasterised by one thread, a larger part by a warp (1..2048) */
+    int32_t tiles_y;        /* tiles down (1, 2, 4 or 8), tiles_x * tiles_y <= 8; 0: the
+                             * most that tiles_x allows (8 / tiles_x) */
+} axr_bin_params;
+axr_status axr_set_bin_params(axr_context* ctx, const axr_bin_params* params);
+axr_status axr_get_bin_params(const axr_context* ctx, axr_bin_params* out);
+
 /* No counterpart in the reference. The same draw as axr_draw_mesh for callers that cannot
  * allocate device memory: a renderer recording its frame into a CUDA graph, a real-time
  * loop that forbids allocator calls after start-up, or a host that owns the device-memory
@@ -307,8 +339,10 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
  * reserved on every GPU that loads the library until exit), so the call allocates nothing.
  * Limits: 65536 vertices, 65536 drawn faces, 1024*1024 framebuffer pixels; larger draws
  * return AXR_E_CAPACITY. The first call on a device looks up the array's address, so make
- * it before any stream capture. All calls share the array: calls whose work overlaps on
- * the GPU (other streams or contexts) race. */
+ * it before any stream capture; the address is kept until exit, so do not use this entry
+ * point after a cudaDeviceReset. All calls share the array: calls whose work overlaps on
+ * the GPU (other streams or contexts) race. Device error bits and statistics reach
+ * axr_sync and axr_stats_read as for axr_draw_mesh; stage profiles leave the call out. */
 axr_status axr_draw_mesh_noalloc(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
 
 /* ------------------------------------------------------------------ batched form
@@ -355,6 +389,12 @@ void axr_batch_destroy(axr_context* ctx, axr_batch* batch);
  * back into its stream, also inside a graph capture), so that the sets' phases overlap. */
 #define AXR_BATCH_PERSISTENT 0
 #define AXR_BATCH_PHASED 1
+/* BINNED: three launches per shader kind over the work units of every draw: vertices,
+ * faces (setup and binning, as axr_draw_mesh's binned form) and bins (raster, shading and
+ * write-out of one bin of 8 tiles per CTA, the draw's clears fused into it); bin
+ * parameters per density class from axr_batch_set_bin_tuning. Large batches run as two
+ * launch sets like PHASED. */
+#define AXR_BATCH_BINNED 2
 axr_status axr_batch_set_form(axr_context* ctx, int32_t form);
 int32_t axr_batch_get_form(const axr_context* ctx);
 
@@ -389,6 +429,9 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
                               int32_t out_small_max_pixels[AXR_TUNE_CLASSES]);
 axr_status axr_batch_get_tuning(const axr_context* ctx, int32_t small_max_pixels[AXR_TUNE_CLASSES]);
 axr_status axr_batch_set_tuning(axr_context* ctx, const int32_t small_max_pixels[AXR_TUNE_CLASSES]);
+/* Bin parameters per density class of the binned form (capacity 16..65536, never 0). */
+axr_status axr_batch_get_bin_tuning(const axr_context* ctx, axr_bin_params out[AXR_TUNE_CLASSES]);
+axr_status axr_batch_set_bin_tuning(axr_context* ctx, const axr_bin_params params[AXR_TUNE_CLASSES]);
 /* Density class of one draw (the classification the planner uses). */
 int32_t axr_draw_density_class(const axr_draw_desc* draw);
 

@@ -68,3 +68,37 @@ def test_noalloc_draw_rejects_oversized_target():
     assert status == AXR_E_CAPACITY
     assert b"limited to" in ctx.lib.axr_last_error(ctx.handle)
     ctx.close()
+
+
+def test_noalloc_draw_reports_statistics_and_allocates_nothing():
+    """The no-allocation draw's statistics reach axr_stats_read (the same triangle and
+    fragment counts as the keyed per-draw path, which runs the same kernels; the kernel
+    that adds them to the context's counters carries the error bits the same way), and
+    after one warm-up call further calls leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    ctx = api.Context(0)
+    sc = W.sphere_scene(width=320, height=240, lon=96, lat=48, tex_size=64)
+    ctx.draw_form = api.DRAW_KEYED
+    ctx.stats(True)
+    ctx.stats()
+    draw(ctx, sc, "axr_draw_mesh")
+    regular = ctx.stats()
+    draw(ctx, sc, "axr_draw_mesh_noalloc")
+    noalloc = ctx.stats()
+    assert noalloc["triangles"] == regular["triangles"] > 0
+    assert noalloc["fragments"] == regular["fragments"] > 0
+    ctx.stats(False)
+    # free device memory across the calls (the framebuffer and mesh are made first)
+    fb = api.Framebuffer(ctx, sc.width, sc.height)
+    mesh = api.Mesh.from_workload(ctx, sc.mesh)
+    pipe = api.TiledPipeline(ctx, api.Camera.from_workload(sc.camera), fb)
+    pipe.setShader(api.BlinnPhongShader())
+    model = np.ascontiguousarray(sc.model, np.float32)
+    assert ctx.lib.axr_draw_mesh_noalloc(ctx.handle, mesh.handle, model.ctypes.data) == 0
+    ctx.sync()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(3):
+        assert ctx.lib.axr_draw_mesh_noalloc(ctx.handle, mesh.handle, model.ctypes.data) == 0
+    ctx.sync()
+    assert torch.cuda.mem_get_info(0)[0] == free0
+    ctx.close()
