@@ -7,7 +7,9 @@ The CUDA runtime is linked statically and its symbols are kept private to the li
 """
 from __future__ import annotations
 
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 from concurrent.futures import ThreadPoolExecutor
@@ -44,11 +46,22 @@ def _deps():
     return sorted(CSRC.glob("*")) + [ROOT / "include" / "axr.h", Path(__file__)]
 
 
+def _digest() -> str:
+    """Content hash of every input of the library (sources, headers, this recipe, the extra
+    compiler flags and the host architecture): the library is rebuilt when it changes."""
+    h = hashlib.sha256()
+    for p in _deps():
+        if p.is_file():
+            h.update(p.name.encode())
+            h.update(p.read_bytes())
+    h.update(os.environ.get("AXR_NVCC_FLAGS", "").encode())
+    h.update(platform.machine().encode())
+    return h.hexdigest()
+
+
 def _stale(out: Path) -> bool:
-    if not out.exists():
-        return True
-    t = out.stat().st_mtime
-    return any(p.stat().st_mtime > t for p in _deps() if p.is_file())
+    stamp = out.with_suffix(".sha256")
+    return not out.exists() or not stamp.exists() or stamp.read_text().strip() != _digest()
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
@@ -87,6 +100,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
           "-Xlinker", "--exclude-libs,ALL", "-Xlinker", f"--version-script={CSRC / 'exports.map'}",
           "-lpthread", "-ldl", "-lrt"])
     tmp.replace(LIB)
+    LIB.with_suffix(".sha256").write_text(_digest() + "\n")
     (OUT_DIR / "ptxas.log").write_text("\n".join(logs))
     if verbose:
         print("\n".join(logs))

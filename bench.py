@@ -520,8 +520,8 @@ def batch_algo_bytes(scenes, frags: float) -> float:
 
 
 def binned_phase_bytes(scenes, shaded: float) -> dict:
-    """Algorithmic bytes of each phase of one step in the binned form, SURVEY-style frame
-    bytes split by the phase that moves them: the vertex attributes read (32 per vertex:
+    """Algorithmic bytes of each phase of one step in the binned form, the frame's bytes
+    split by the phase that moves them: the vertex attributes read (32 per vertex:
     position, normal, uv) by the vertex phase, the indices (12 per face) by the face phase,
     and one colour + one depth write per pixel (8) plus min(texture bytes, 4 per shaded
     fragment) by the bin pass. Their sum is the frame roofline's bytes; the intermediate
@@ -831,7 +831,7 @@ def run_batch(args, dist: Dist):
     ms = total_ms / len(step_ms)
     frags = float(st["fragments"])
     algo = batch_algo_bytes(scenes, frags)
-    # fragment ALU work (SURVEY's frame roofline): FP32 operations of the Blinn-Phong
+    # fragment ALU work (the frame roofline's ALU side): FP32 operations of the Blinn-Phong
     # fragment functor counted from its source (K_BLINN_PHONG) per shaded fragment, plus
     # three edge evaluations and three compares (9) per tested pixel
     alu_flop = K_BLINN_PHONG * float(st["shaded"]) + 9.0 * float(st["tested"])

@@ -4,7 +4,7 @@
   ``oracle/_build/libaxo_port.so``. It builds on any host (x86 here, aarch64 on the GPU
   box) and is the checker the GPU parity tests and the CPU baseline use.
 * ``build_ref()`` compiles the AxiomR reference sources *where they lie* (the reference
-  tree, default ``/root/reference``, override with ``AXR_REFERENCE``) together with the
+  tree: ``AXR_REFERENCE``, else ``reference`` beside the repository root) together with the
   project's shims in ``oracle/shim`` and ``oracle/ref_harness.cpp`` into
   ``oracle/_ref/libaxr_ref.so``. No reference source is copied. The reference's
   rasteriser uses AVX2 (and contains unused AVX-512 variants), so this build is x86-only;
@@ -54,7 +54,8 @@ ALIASES = {
 
 
 def reference_root() -> Path:
-    return Path(os.environ.get("AXR_REFERENCE", "/root/reference"))
+    env = os.environ.get("AXR_REFERENCE")
+    return Path(env) if env else HERE.parent.parent / "reference"
 
 
 def _run(cmd: list[str]) -> None:
