@@ -138,7 +138,7 @@ struct axr_context {
                                                  {256, 4, 64, 2}, {256, 4, 64, 2}, {256, 4, 64, 2}};
     // binned per-draw form (axr_draw_mesh): its parameters and scratch: the bin counters
     // followed by the bin counts, the bins' entries and the clipped-triangle records
-    int draw_form = AXR_DRAW_BINNED;
+    int draw_form = AXR_DRAW_KEYED;
     axr_bin_params bin_params{0, 0, 64, 0};
     axr::BinCounters* bin_mem = nullptr;
     uint32_t* bin_entries = nullptr;

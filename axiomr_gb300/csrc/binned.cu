@@ -13,7 +13,7 @@ namespace {
 constexpr int kBlock = 256;
 
 // Resident CTAs per SM the bin kernel is compiled for (5: at most 48 registers; its shared
-// memory, about 37 KB per CTA, allows 6).
+// memory, about 38 KB per CTA, allows 5 as well).
 #ifndef AXR_BIN_MIN_BLOCKS
 #define AXR_BIN_MIN_BLOCKS 5
 #endif

@@ -131,26 +131,52 @@ __device__ __forceinline__ void raster_rect_thread(const Edges& e, uint32_t tag,
     }
 }
 
-// The same over a rectangle by the whole warp: its pixels in row-major order, lane-strided,
-// each evaluated on its own (eval_pixel derives the row start from the pixel).
-__device__ __forceinline__ void raster_rect_warp(const Edges& e, uint32_t tag, const PixRect& r, int X0, int Y0, int tw,
-                                 unsigned long long* keys, uint32_t& frags, uint32_t& tested) {
-    const int lane = threadIdx.x & 31;
-    const int rw = r.x1 - r.x0, n = rw * (r.y1 - r.y0);
-    int px = r.x0 + lane % rw, py = r.y0 + lane / rw;
-    const int dx = 32 % rw, dy = 32 / rw;
-    for (int i = lane; i < n; i += 32) {
-        ++tested;
-        const PixelEval pe = eval_pixel(e, px, py);
-        if (pe.covered) {
-            ++frags;
-            if (pe.z < __int_as_float(0x7f800000)) key_min(&keys[bin_slot(px, py, X0, Y0, tw)], make_key(pe.z, tag));
+// Smallest power of two >= v (v >= 1).
+__device__ __forceinline__ int pow2_ceil(int v) { return v <= 1 ? 1 : 1 << (32 - __clz(v - 1)); }
+
+// The same over a rectangle by a group of G threads (a warp: G = 32; the CTA: G = 256),
+// `t` the thread's index in the group. The group covers wp = min(G, next power of two >=
+// width) columns and G / wp rows at a time, so neighbouring threads touch neighbouring keys;
+// a thread's column terms of eval_pixel (a*(sx+0.5) at the reference's row start sx, a*8,
+// a*(offset in the 8-pixel block)) are computed once per column, then each row costs
+// b*(y+0.5) and the adds, in eval_pixel's order.
+template <int G>
+__device__ __forceinline__ void raster_rect_group(const Edges& e, uint32_t tag, const PixRect& r, int X0, int Y0,
+                                                  int tw, unsigned long long* keys, int t, uint32_t& frags,
+                                                  uint32_t& tested) {
+    const int wp = min(G, pow2_ceil(r.x1 - r.x0));
+    const int col = t & (wp - 1), row0 = t / wp, rpp = G / wp;
+    for (int xs = r.x0; xs < r.x1; xs += wp) {
+        const int px = xs + col;
+        if (px >= r.x1) continue;
+        const int sx = max(px & ~(kTile - 1), e.x_lo);
+        const int i = px - sx;
+        const float fsx = fadd((float)sx, 0.5f), fl = (float)(i & 7);
+        const bool hi = i >= 8;
+        float as[3], al[3], a8[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            as[k] = fmul(e.a[k], fsx);
+            al[k] = fmul(e.a[k], fl);
+            a8[k] = fmul(e.a[k], 8.0f);
         }
-        px += dx;
-        py += dy;
-        if (px >= r.x1) {
-            px -= rw;
-            ++py;
+        for (int py = r.y0 + row0; py < r.y1; py += rpp) {
+            ++tested;
+            const float fpy = fadd((float)py, 0.5f);
+            float cov[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float row = fadd(fadd(as[k], fmul(e.b[k], fpy)), e.c[k]);
+                if (hi) row = fadd(row, a8[k]);
+                cov[k] = fadd(row, al[k]);
+            }
+            if (cov[0] >= 0.f && cov[1] >= 0.f && cov[2] >= 0.f) {
+                ++frags;
+                const float al_ = fmul(cov[0], e.inv_area), be = fmul(cov[1], e.inv_area),
+                            ga = fmul(cov[2], e.inv_area);
+                const float z = fadd(fadd(fmul(e.z[0], al_), fmul(e.z[1], be)), fmul(e.z[2], ga));
+                if (z < __int_as_float(0x7f800000)) key_min(&keys[bin_slot(px, py, X0, Y0, tw)], make_key(z, tag));
+            }
         }
     }
 }
@@ -359,11 +385,12 @@ struct BinSmem {
     unsigned long long key[kBinTiles][256];  // depth keys of the bin's pixels
     __align__(128) uint32_t col[kBinTiles][256];  // colour staging, one 16x16 TMA box per tile
     __align__(128) float dep[kBinTiles][256];     // depth staging
-    uint32_t wide[2][kBinThreads];                // entries left to the warp rasteriser, by round parity
-    uint8_t win[kBinTiles][256];                  // winner pixels of each tile
-    uint32_t wcnt[kBinTiles][kBinThreads / 32];   // winners per tile and warp (compaction)
-    uint32_t nwin[kBinTiles];
-    uint32_t n_wide[3];                           // wide-queue fill, by round modulo 3
+    uint32_t wide[2][kBinThreads];                // entries left to the warp (front) and CTA (back)
+                                                  // rasterisers, by round parity
+    uint16_t wl[kBinThreads / 32][kBinTiles * 32]; // each warp's winners: tile << 8 | pixel
+    uint32_t tile_has;                            // bit k: tile k has a winner
+    uint32_t n_med[3], n_big[3];                  // queue fills, by round modulo 3
+    uint32_t grab[2];                             // next warp-sized entry to hand out, by round parity
     uint32_t ok;
     uint64_t bar;                                 // arrival of the tile loads
 };
@@ -452,10 +479,14 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
     }
     const bool tma = (flags & kBatchTma) != 0u;
     const bool load_c = !clear_c, load_d = !clear_d;
+    const uint32_t* list = b.entries + (size_t)lb * b.cap;
+    uint32_t next = (uint32_t)tid < n ? __ldg(list + tid) : 0u;  // round 0's entry, in flight during set-up
     if (tid == 0) {
-        sm.n_wide[0] = 0u;
-        sm.n_wide[1] = 0u;
+        sm.n_med[0] = sm.n_med[1] = 0u;
+        sm.n_big[0] = sm.n_big[1] = 0u;
+        sm.grab[0] = sm.grab[1] = 0u;
         sm.ok = 1u;
+        sm.tile_has = 0u;
         mbar_init(&sm.bar, 1);
         mbar_fence_init();
     }
@@ -486,13 +517,13 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
     }
     __syncthreads();
 
-    // ---- rasterise the bin's entries, kBinThreads per round; one barrier per round: the
-    // wide queue alternates between two buffers, its fill counter among three (round r
-    // clears the counter of round r + 2 after its barrier)
+    // ---- rasterise the bin's entries, kBinThreads per round. A triangle's part of the bin
+    // of at most thread_px pixels is rasterised by its thread, up to 256 pixels by a warp,
+    // larger by the whole CTA. One barrier per round: the queues alternate between two
+    // buffers (warp entries from the front, CTA entries from the back), their fill counters
+    // among three (round r clears the counters of round r + 2 after its barrier).
     uint32_t frags = 0, tested = 0, wides = 0;
     unsigned long long* keys = &sm.key[0][0];
-    const uint32_t* list = b.entries + (size_t)lb * b.cap;
-    uint32_t next = (uint32_t)tid < n ? __ldg(list + tid) : 0u;
     uint32_t round = 0;
     for (uint32_t base = 0; base < n; base += kBinThreads, ++round) {
         const uint32_t q = base + (uint32_t)tid;
@@ -503,29 +534,48 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
             const uint32_t tag = load_entry(p, bs, entry, e);
             const PixRect r = clip_rect(R, e);
             if (r.x0 < r.x1 && r.y0 < r.y1) {
-                if ((r.x1 - r.x0) * (r.y1 - r.y0) <= (int)b.thread_px)
+                const int npx = (r.x1 - r.x0) * (r.y1 - r.y0);
+                if (npx <= (int)b.thread_px)
                     raster_rect_thread(e, tag, r, R.x0, R.y0, tw, keys, frags, tested);
+                else if (npx <= 256)
+                    sm.wide[round & 1][atomicAdd(&sm.n_med[round % 3], 1u)] = entry;
                 else
-                    sm.wide[round & 1][atomicAdd(&sm.n_wide[round % 3], 1u)] = entry;
+                    sm.wide[round & 1][kBinThreads - 1 - atomicAdd(&sm.n_big[round % 3], 1u)] = entry;
             }
         }
         __syncthreads();
-        const uint32_t nw = sm.n_wide[round % 3];
-        if (tid == 0) sm.n_wide[(round + 2) % 3] = 0u;
-        wides += nw;
-        for (uint32_t k = (uint32_t)warp; k < nw; k += kBinThreads / 32) {
+        const uint32_t nm = sm.n_med[round % 3], nb = sm.n_big[round % 3];
+        if (tid == 0) {
+            sm.n_med[(round + 2) % 3] = sm.n_big[(round + 2) % 3] = 0u;
+            sm.grab[(round + 1) & 1] = 0u;  // last used in round r - 1, whose grabs ended before this barrier
+        }
+        wides += nm + nb;
+        // CTA-wide triangles first (every warp takes part in each), then the warp-sized ones
+        // handed out one at a time to whichever warp is free
+        for (uint32_t k = 0; k < nb; ++k) {
+            const uint32_t we = sm.wide[round & 1][kBinThreads - 1 - k];
+            Edges e;
+            const uint32_t tag = load_entry(p, bs, we, e);
+            raster_rect_group<kBinThreads>(e, tag, clip_rect(R, e), R.x0, R.y0, tw, keys, tid, frags, tested);
+        }
+        for (;;) {
+            uint32_t k = 0;
+            if (lane == 0) k = atomicAdd(&sm.grab[round & 1], 1u);
+            k = __shfl_sync(kFullMask, k, 0);
+            if (k >= nm) break;
             const uint32_t we = sm.wide[round & 1][k];
             Edges e;
             const uint32_t tag = load_entry(p, bs, we, e);
-            raster_rect_warp(e, tag, clip_rect(R, e), R.x0, R.y0, tw, keys, frags, tested);
+            raster_rect_group<32>(e, tag, clip_rect(R, e), R.x0, R.y0, tw, keys, lane, frags, tested);
         }
     }
     __syncthreads();
 
-    // ---- winners: keys spilled into the key plane folded in first, then the winner pixels
-    // of each tile compacted in pixel order (ballots, then a prefix over the warps)
+    // ---- winners, per warp: keys spilled into the key plane folded in first, then the warp's
+    // winner pixels (its two rows of every tile: coverage spreads evenly over the warps)
+    // compacted by ballots into its own list and shaded by the warp
     const unsigned below = (1u << lane) - 1u;
-    unsigned has_mask = 0u;  // bit k: this thread's pixel of tile k has a winner
+    uint32_t nw = 0;  // winners of this warp
     for (int k = 0; k < nt; ++k) {
         const int ox = tile_x(k), oy = tile_y(k), px = ox + lx, py = oy + ly;
         const bool in = ox < t.width && oy < t.height && px < t.width && py < t.height;
@@ -543,57 +593,35 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
             }
         }
         const bool has = in && key != kEmptyKey;
-        has_mask |= has ? (1u << k) : 0u;
         const unsigned m = __ballot_sync(kFullMask, has);
-        if (lane == 0) sm.wcnt[k][warp] = (uint32_t)__popc(m);
+        if (has) sm.wl[warp][nw + (uint32_t)__popc(m & below)] = (uint16_t)((k << 8) | tid);
+        nw += (uint32_t)__popc(m);
+        if (m && lane == 0) atomicOr(&sm.tile_has, 1u << k);
         if (clear_c) sm.col[k][tid] = clear_bgra;
         if (clear_d) sm.dep[k][tid] = clear_depth;
     }
     // the loaded planes must have arrived before the merge test reads them
+    bool loaded = true;
     if (tma && (load_c || load_d) && !mbar_wait_bounded(&sm.bar, 0)) {
         atomicOr(&counters->error, kErrTma);
         sm.ok = 0u;
+        loaded = false;
     }
-    __syncthreads();
-    if (spilled && tid < nt) {  // flags of the folded tiles back to zero (after every read)
-        const int ox = tile_x(tid), oy = tile_y(tid);
-        if (ox < t.width && oy < t.height) t.tile_flag[(uint32_t)(oy >> 4) * (uint32_t)t.tiles_x + (uint32_t)(ox >> 4)] = 0u;
-    }
-    if (!sm.ok) return;  // tile contents unknown: leave the framebuffer as it is
-    for (int k = 0; k < nt; ++k) {
-        uint32_t off = 0;
-        for (int w = 0; w < warp; ++w) off += sm.wcnt[k][w];
-        const unsigned m = __ballot_sync(kFullMask, (has_mask >> k) & 1u);
-        if ((has_mask >> k) & 1u) sm.win[k][off + (uint32_t)__popc(m & below)] = (uint8_t)tid;
-        if (tid == 0) {
-            uint32_t tot = 0;
-            for (int w = 0; w < kBinThreads / 32; ++w) tot += sm.wcnt[k][w];
-            sm.nwin[k] = tot;
-        }
-    }
-    __syncthreads();
-
-    // ---- shade the winners of all tiles, spread over the CTA
-    uint32_t pre[kBinTiles + 1];
-    pre[0] = 0;
-#pragma unroll
-    for (int w = 0; w < kBinTiles; ++w) pre[w + 1] = pre[w] + (w < nt ? sm.nwin[w] : 0u);
-    const uint32_t total = pre[kBinTiles];
-    for (uint32_t q = (uint32_t)tid; q < total; q += kBinThreads) {
-        int w = 0;
-#pragma unroll
-        for (int k = 1; k < kBinTiles; ++k) w += q >= pre[k] ? 1 : 0;
-        const uint32_t pix = sm.win[w][q - pre[w]];
-        const uint32_t tag = (uint32_t)sm.key[w][pix];
-        const int gx = tile_x(w) + (int)(pix & 15u), gy = tile_y(w) + (int)(pix >> 4);
-        const float old = clear_d ? clear_depth : sm.dep[w][pix];
+    __syncwarp();
+    for (uint32_t q = (uint32_t)lane; loaded && q < nw; q += 32) {
+        const uint32_t v = sm.wl[warp][q];
+        const int k = (int)(v >> 8);
+        const uint32_t pix = v & 255u;
+        const uint32_t tag = (uint32_t)sm.key[k][pix];
+        const int gx = tile_x(k) + (int)(pix & 15u), gy = tile_y(k) + (int)(pix >> 4);
+        const float old = clear_d ? clear_depth : sm.dep[k][pix];
         uint32_t bgra = 0u;
         float z = 0.0f;
         const bool ok = (tag & 8u) ? shade_clipped_px<S>(p, tag, gx, gy, old, &bgra, &z)
                                    : shade_unclipped<S, false>(p, tag, gx, gy, old, bgra, z);
         if (ok) {
-            sm.col[w][pix] = bgra;
-            sm.dep[w][pix] = z;
+            sm.col[k][pix] = bgra;
+            sm.dep[k][pix] = z;
         }
     }
     if (stats) {
@@ -601,13 +629,20 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
         if (lane == 0) {
             if (f) atomicAdd(&counters->stat_fragments, (unsigned long long)f);
             if (te) atomicAdd(&counters->stat_tested, (unsigned long long)te);
+            if (nw) atomicAdd(&counters->stat_shaded, (unsigned long long)nw);
         }
         if (tid == 0) {
             atomicAdd(&counters->stat_tiles, 1ull);
-            atomicAdd(&counters->stat_shaded, (unsigned long long)total);
             if (wides) atomicAdd(&counters->stat_large, (unsigned long long)wides);
         }
     }
+    __syncthreads();
+    if (spilled && tid < nt) {  // flags of the folded tiles back to zero (after every read)
+        const int ox = tile_x(tid), oy = tile_y(tid);
+        if (ox < t.width && oy < t.height) t.tile_flag[(uint32_t)(oy >> 4) * (uint32_t)t.tiles_x + (uint32_t)(ox >> 4)] = 0u;
+    }
+    if (!sm.ok) return;  // tile contents unknown: leave the framebuffer as it is
+    const uint32_t tile_has = sm.tile_has;
 
     // ---- write the tiles out: a plane of a tile is written when it was cleared or the tile
     // has winners
@@ -618,8 +653,9 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
             for (int k = 0; k < nt; ++k) {
                 const int x = tile_x(k), y = tile_y(k);
                 if (x >= t.width || y >= t.height) continue;
-                if (clear_c || sm.nwin[k]) tma_store_tile(cmap, sm.col[k], x, y);
-                if (clear_d || sm.nwin[k]) tma_store_tile(dmap, sm.dep[k], x, y);
+                const bool any = (tile_has >> k) & 1u;
+                if (clear_c || any) tma_store_tile(cmap, sm.col[k], x, y);
+                if (clear_d || any) tma_store_tile(dmap, sm.dep[k], x, y);
             }
             tma_commit();
             tma_wait_read_0();  // shared memory is released when the CTA exits
@@ -631,7 +667,7 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
         const int px = tile_x(k) + lx, py = tile_y(k) + ly;
         if (px >= t.width || py >= t.height) continue;
         const size_t idx = (size_t)py * (size_t)t.width + (size_t)px;
-        const bool any = sm.nwin[k] != 0u;
+        const bool any = (tile_has >> k) & 1u;
         if (clear_c || any) t.color[idx] = sm.col[k][tid];
         if (clear_d || any) t.depth[idx] = sm.dep[k][tid];
     }

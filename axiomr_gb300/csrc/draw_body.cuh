@@ -503,6 +503,19 @@ namespace {
 // Fragment of the unclipped winner `tag` at (px, py): the setup from its shading record
 // when it has one, else re-derived from the face; then exact barycentrics and depth, the
 // strict merge test against `old_depth` and the shader. Returns whether it is written.
+// Fragment at (px, py) of a triangle given its setup, vertex-shader outputs and material:
+// exact barycentrics and depth, the strict merge test against `old_depth` and the shader.
+template <int S>
+__device__ __forceinline__ bool shade_from(const DrawParams& p, const Edges& e, const VSOut* vo, uint32_t material,
+                                           int px, int py, float old_depth, uint32_t& bgra, float& z) {
+    const PixelEval r = eval_pixel(e, px, py);
+    if (!(r.z < old_depth)) return false;
+    const f4 col = fragment_shader<S>(p.u, p.mesh.materials[material], mk3(r.alpha, r.beta, r.gamma), vo);
+    bgra = pack_bgra(col);
+    z = r.z;
+    return true;
+}
+
 template <int S, bool kCoherent = false>
 __device__ __forceinline__ bool shade_unclipped(const DrawParams& p, uint32_t tag, int px, int py, float old_depth,
                                                 uint32_t& bgra, float& z) {
@@ -516,12 +529,7 @@ __device__ __forceinline__ bool shade_unclipped(const DrawParams& p, uint32_t ta
         material = winner_inputs<S, kCoherent>(p, tag, s, vo);
         if (!edge_setup(s, p.target.width, p.target.height, e)) return false;
     }
-    const PixelEval r = eval_pixel(e, px, py);
-    if (!(r.z < old_depth)) return false;
-    const f4 col = fragment_shader<S>(p.u, p.mesh.materials[material], mk3(r.alpha, r.beta, r.gamma), vo);
-    bgra = pack_bgra(col);
-    z = r.z;
-    return true;
+    return shade_from<S>(p, e, vo, material, px, py, old_depth, bgra, z);
 }
 
 // Winner that came out of the clipper: its inputs from the clipper re-run, then the

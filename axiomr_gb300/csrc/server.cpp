@@ -111,6 +111,9 @@ struct Req {
 };
 
 struct Slot {
+    // the slot's own context: its stream, work counters and draw scratch, so that the
+    // kernels of batches in different slots run side by side
+    axr_context* sctx = nullptr;
     axr_batch plan;
     std::vector<Req*> reqs;
     cudaEvent_t kernel_done = nullptr, copies_done = nullptr;
@@ -132,6 +135,7 @@ struct axr_server {
     axr_context* ctx = nullptr;
     cudaStream_t upload = nullptr, copy = nullptr;
     cudaEvent_t uploaded = nullptr;
+    cudaEvent_t home_ready = nullptr;  // the home stream's allocations and frees so far
     std::vector<std::unique_ptr<TexAsset>> textures;
     std::vector<std::unique_ptr<MeshAsset>> meshes;
     std::vector<std::unique_ptr<Fb>> fbs;
@@ -411,6 +415,7 @@ struct axr_server {
         const uint64_t t = steady_ns();
         for (Req* q : s.reqs) q->launch = t;
         cudaError_t e = cudaSuccess;
+        axr_context* ctx = s.sctx;  // the slot's stream and scratch
         if (cfg.per_request) {
             // the per-draw path for each request: clears, then drawMesh (tiled_pipeline.cpp:143)
             for (Req* q : s.reqs) {
@@ -583,10 +588,14 @@ struct axr_server {
                     free_slot->reqs.push_back(q);
                 }
                 if (!free_slot->reqs.empty()) {
-                    cudaError_t e = cudaSuccess;
-                    if (did_upload) {
+                    // the slot's stream waits for the uploads and for the home stream's
+                    // framebuffer allocations and frees
+                    cudaStream_t ss = free_slot->sctx->stream;
+                    cudaError_t e = cudaEventRecord(home_ready, ctx->stream);
+                    if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, home_ready, 0);
+                    if (e == cudaSuccess && did_upload) {
                         e = cudaEventRecord(uploaded, upload);
-                        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, uploaded, 0);
+                        if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, uploaded, 0);
                     }
                     free_slot->id = next_batch++;
                     for (Req* q : free_slot->reqs) {
@@ -627,8 +636,15 @@ axr_status axr_server_create(const axr_server_config* cfg, axr_server** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&srv->upload, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&srv->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&srv->uploaded, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&srv->home_ready, cudaEventDisableTiming);
     for (int32_t k = 0; k < cfg->max_inflight && e == cudaSuccess; ++k) {
         auto s = std::make_unique<Slot>();
+        st = axr_context_create(cfg->device, &s->sctx);
+        if (st != AXR_OK) {
+            srv->slots.push_back(std::move(s));
+            axr_server_destroy(srv.release());
+            return st;
+        }
         e = cudaEventCreateWithFlags(&s->kernel_done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->copies_done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->files_done, cudaEventDisableTiming);
@@ -666,15 +682,18 @@ void axr_server_destroy(axr_server* srv) {
             if (t->dev.texels) cudaFreeAsync(const_cast<uint32_t*>(t->dev.texels), srv->ctx->stream);
         for (auto& f : srv->fbs) srv->free_fb(*f);
         for (auto& s : srv->slots) {
+            if (s->sctx) cudaStreamSynchronize(s->sctx->stream);
             free_batch(&s->plan);
             free_batch_staging(&s->plan);
             if (s->kernel_done) cudaEventDestroy(s->kernel_done);
             if (s->copies_done) cudaEventDestroy(s->copies_done);
             if (s->files_done) cudaEventDestroy(s->files_done);
             for (axr_png_batch* b : s->png) png_batch_release(b);
+            if (s->sctx) axr_context_destroy(s->sctx);
         }
         cudaStreamSynchronize(srv->ctx->stream);
         if (srv->uploaded) cudaEventDestroy(srv->uploaded);
+        if (srv->home_ready) cudaEventDestroy(srv->home_ready);
         if (srv->copy) cudaStreamDestroy(srv->copy);
         if (srv->upload) cudaStreamDestroy(srv->upload);
         axr_context_destroy(srv->ctx);

@@ -76,7 +76,7 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true", help="batch: plan with the default tuning table")
     ap.add_argument("--form", choices=("auto", "persistent", "phased", "binned"), default="auto",
                     help="batch: launch form (auto: the autotuner's choice)")
-    ap.add_argument("--draw-form", choices=("binned", "keyed"), default="binned",
+    ap.add_argument("--draw-form", choices=("binned", "keyed"), default="keyed",
                     help="single-draw workloads: form of the per-draw path")
     ap.add_argument("--draws", type=int, default=512, help="batch: number of draws (a smaller batch for profiling)")
     ap.add_argument("--scale", type=float, default=1.0, help="batch: framebuffer size scale (profiling)")
@@ -977,9 +977,17 @@ def serve_sweep(device: int, rates, seconds: float, budget_gb: float, readback: 
         def out(buf):
             return {"png_channels": 3, "out_png": buf} if readback == "png" else {"out_bgra": buf}
 
-        # warm-up: every asset resident once, framebuffer pools filled
+        # warm-up: every asset resident once, framebuffer pools filled, then two full-size
+        # batches at once so that both in-flight slots have grown their scratch
         ts = [srv.submit(*r, **out(ring[k % len(ring)])) for k, r in enumerate(reqs)]
         ts.append(srv.submit(hf_id, api.Camera.from_workload(hf.camera), blinn, 1920, 1080, **out(hf_ring[0])))
+        for t in ts:
+            srv.wait(t)
+        srv.hold(True)
+        ts = [srv.submit(*reqs[k % len(reqs)], **out(ring[k % len(ring)])) for k in range(2 * 64 - 2)]
+        ts += [srv.submit(hf_id, api.Camera.from_workload(hf.camera), blinn, 1920, 1080, **out(hf_ring[k]))
+               for k in range(2)]
+        srv.hold(False)
         for t in ts:
             srv.wait(t)
         per_rate = []

@@ -301,7 +301,9 @@ axr_status axr_set_framebuffer(axr_context* ctx, axr_framebuffer* fb);
 axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float model[16]);
 
 /* Forms of axr_draw_mesh; no counterpart in the reference, both give its frame.
- * BINNED (the default): the reference's binTrianglesToTiles / processTile /
+ * KEYED is the default: on one large draw (2M triangles at 1920x1080, 200k at 3840x2160)
+ * it measured faster; BINNED was faster on a small one (4k triangles at 512x512).
+ * BINNED: the reference's binTrianglesToTiles / processTile /
  * mergeTileResults (src/tiled_pipeline.cpp:368-425, 1125-1181) on the GPU. A face kernel
  * sets up every triangle and appends it to the entry list of each bin of 8 tiles (16x16)
  * that its box reaches; one CTA per bin then rasterises the bin's list into depth keys in

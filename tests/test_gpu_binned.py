@@ -1,5 +1,5 @@
 """The binned forms (bins of 8 tiles rasterised in shared memory, TMA tile loads and
-stores): the per-draw binned path (axr_draw_mesh's default) must give exactly the frame of
+stores): the per-draw binned path (AXR_DRAW_BINNED) must give exactly the frame of
 the keyed path (visibility keys in device memory), whatever the bin shape, per-thread raster
 limit or bin capacity (a full bin spills into the key plane), whether the framebuffer is
 cleared, pre-filled or drawn into several times, and whether its width allows tensor maps;
@@ -31,7 +31,7 @@ def render(ctx, form, scene, params=None, **kw):
     try:
         return api.render_scene(ctx, scene, **kw)
     finally:
-        ctx.draw_form = api.DRAW_BINNED
+        ctx.draw_form = api.DRAW_KEYED
         ctx.bin_params = {"capacity": 0, "tiles_x": 0, "tiles_y": 0, "thread_pixels": 64}
 
 
@@ -105,7 +105,7 @@ def test_several_draws_into_one_framebuffer(ctx):
             pipe.drawMesh(sc.model, api.Mesh.from_workload(ctx, sc.mesh))
         results[form] = fb.read()
         fb.close()
-    ctx.draw_form = api.DRAW_BINNED
+    ctx.draw_form = api.DRAW_KEYED
     same(results[api.DRAW_BINNED], results[api.DRAW_KEYED], "three draws into one framebuffer")
 
 
