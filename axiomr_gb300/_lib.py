@@ -109,7 +109,7 @@ class DrawStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("memory_budget_bytes", C.c_uint64), ("max_batch", C.c_int32),
-                ("max_inflight", C.c_int32), ("per_request", C.c_int32), ("pad_", C.c_int32)]
+                ("max_inflight", C.c_int32), ("per_request", C.c_int32), ("overlap_kernels", C.c_int32)]
 
 
 class ServerMaterial(C.Structure):

@@ -693,10 +693,10 @@ class Server:
     render requests, wait for their results. Latency is measured on the server clock."""
 
     def __init__(self, device: int = 0, budget_bytes: int = 40 << 30, max_batch: int = 64, max_inflight: int = 2,
-                 per_request: bool = False):
+                 per_request: bool = False, overlap_kernels: bool = False):
         self.lib = _lib.load()
         cfg = _lib.ServerConfig(int(device), int(budget_bytes), int(max_batch), int(max_inflight),
-                                1 if per_request else 0, 0)
+                                1 if per_request else 0, 1 if overlap_kernels else 0)
         h = C.c_void_p()
         st = self.lib.axr_server_create(C.byref(cfg), C.byref(h))
         if st != 0:

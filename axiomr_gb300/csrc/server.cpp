@@ -111,8 +111,9 @@ struct Req {
 };
 
 struct Slot {
-    // the slot's own context: its stream, work counters and draw scratch, so that the
-    // kernels of batches in different slots run side by side
+    // with overlap_kernels, the slot's own context: its stream, work counters and draw
+    // scratch, so that the kernels of batches in different slots run side by side;
+    // otherwise null and the slot renders on the server's context
     axr_context* sctx = nullptr;
     axr_batch plan;
     std::vector<Req*> reqs;
@@ -415,7 +416,7 @@ struct axr_server {
         const uint64_t t = steady_ns();
         for (Req* q : s.reqs) q->launch = t;
         cudaError_t e = cudaSuccess;
-        axr_context* ctx = s.sctx;  // the slot's stream and scratch
+        axr_context* ctx = s.sctx ? s.sctx : this->ctx;  // the stream and scratch the slot renders on
         if (cfg.per_request) {
             // the per-draw path for each request: clears, then drawMesh (tiled_pipeline.cpp:143)
             for (Req* q : s.reqs) {
@@ -588,11 +589,14 @@ struct axr_server {
                     free_slot->reqs.push_back(q);
                 }
                 if (!free_slot->reqs.empty()) {
-                    // the slot's stream waits for the uploads and for the home stream's
-                    // framebuffer allocations and frees
-                    cudaStream_t ss = free_slot->sctx->stream;
-                    cudaError_t e = cudaEventRecord(home_ready, ctx->stream);
-                    if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, home_ready, 0);
+                    // the slot's stream waits for the uploads and, when it is not the home
+                    // stream, for the home stream's framebuffer allocations and frees
+                    cudaStream_t ss = free_slot->sctx ? free_slot->sctx->stream : ctx->stream;
+                    cudaError_t e = cudaSuccess;
+                    if (ss != ctx->stream) {
+                        e = cudaEventRecord(home_ready, ctx->stream);
+                        if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, home_ready, 0);
+                    }
                     if (e == cudaSuccess && did_upload) {
                         e = cudaEventRecord(uploaded, upload);
                         if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, uploaded, 0);
@@ -639,7 +643,7 @@ axr_status axr_server_create(const axr_server_config* cfg, axr_server** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&srv->home_ready, cudaEventDisableTiming);
     for (int32_t k = 0; k < cfg->max_inflight && e == cudaSuccess; ++k) {
         auto s = std::make_unique<Slot>();
-        st = axr_context_create(cfg->device, &s->sctx);
+        st = cfg->overlap_kernels ? axr_context_create(cfg->device, &s->sctx) : AXR_OK;
         if (st != AXR_OK) {
             srv->slots.push_back(std::move(s));
             axr_server_destroy(srv.release());

@@ -459,7 +459,9 @@ typedef struct axr_server_config {
     int32_t max_inflight;         /* batches on the GPU at once (their read-backs overlap) */
     int32_t per_request;          /* 1: render each request alone with the per-draw path
                                      (clearColor, clearDepth, drawMesh), no batching */
-    int32_t pad_;
+    int32_t overlap_kernels;      /* 1: each in-flight slot renders on its own stream and scratch,
+                                     so the kernels of two batches can run side by side; 0: the
+                                     slots share one stream (kernels in order, copies overlapped) */
 } axr_server_config;
 
 /* A texture asset (RGBA8, row 0 first); *out_id receives its id. */
