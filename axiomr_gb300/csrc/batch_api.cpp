@@ -641,7 +641,7 @@ axr_status axr_batch_autotune(axr_context* ctx, const axr_draw_desc* draws, int3
     {
         const int saved_form = ctx->batch_form;
         ctx->batch_form = kFormBinned;
-        static const int32_t kThreadPx[] = {16, 32, 64, 128, 256};
+        static const int32_t kThreadPx[] = {1, 4, 8, 16, 32, 64, 128, 256};
         static const int32_t kShapes[][2] = {{8, 1}, {4, 2}, {2, 4}, {4, 1}, {2, 2}, {2, 1}, {1, 1}};
         static const int32_t kCapacity[] = {64, 128, 256, 512, 1024, 2048};
         for (int k = 0; k < AXR_TUNE_CLASSES && st == AXR_OK; ++k) {

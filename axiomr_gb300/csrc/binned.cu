@@ -12,10 +12,11 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Resident CTAs per SM the bin kernel is compiled for (5: at most 48 registers; its shared
-// memory, about 38 KB per CTA, allows 5 as well).
+// Resident CTAs per SM the bin kernel is compiled for. 4 gives it 64 registers (68 bytes
+// of spills); 5 (48 registers, 256 bytes of spills) measured 6% slower on the 512-draw
+// batch, its spilled locals going to L2 and DRAM beside the tile stores.
 #ifndef AXR_BIN_MIN_BLOCKS
-#define AXR_BIN_MIN_BLOCKS 5
+#define AXR_BIN_MIN_BLOCKS 4
 #endif
 #ifndef AXR_BIN_FACE_MIN_BLOCKS
 #define AXR_BIN_FACE_MIN_BLOCKS 4

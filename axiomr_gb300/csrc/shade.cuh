@@ -25,6 +25,18 @@
 
 namespace axr {
 
+// A texel through the read-only path with an L2 evict_last policy: textures are shared by
+// many draws and re-read across the frame, while the framebuffer planes and per-draw
+// scratch stream through L2 at the default priority. The texel loads are the only reads
+// that carry this policy, so L2's evict_last counters measure exactly the texture fetches.
+__device__ __forceinline__ uint32_t ld_texel(const uint32_t* a) {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    uint32_t v;
+    asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
 __device__ __forceinline__ f4 tex_sample(const DevTexture& t, f2 uv) {
     if (t.texels == nullptr || t.width <= 0) return mk4(0.0f, 0.0f, 0.0f, 1.0f);
     const int w = t.width, h = t.height;
@@ -33,7 +45,7 @@ __device__ __forceinline__ f4 tex_sample(const DevTexture& t, f2 uv) {
     x = max(0, min(x, w - 1));
     y = max(0, min(y, h - 1));
     y = h - 1 - y;
-    uint32_t p = __ldg(&t.texels[(size_t)y * (size_t)w + (size_t)x]);
+    uint32_t p = ld_texel(&t.texels[(size_t)y * (size_t)w + (size_t)x]);
     const float inv255 = 1.0f / 255.0f;
     return mk4(fmul((float)(p & 0xFFu), inv255), fmul((float)((p >> 8) & 0xFFu), inv255),
                fmul((float)((p >> 16) & 0xFFu), inv255), fmul((float)(p >> 24), inv255));

@@ -93,6 +93,9 @@ def parse_args():
                     help="batch: seconds per offered load of the short serving sweep in the line (0: none)")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the device-resident timed steps with cudaProfilerStart/Stop (for ncu "
+                         "--profile-from-start off: -k <kernel> -c 1 then captures a timed launch)")
     return ap.parse_args()
 
 
@@ -345,6 +348,8 @@ def run_ours(args, dist: Dist):
     ctx.sync()
     sampler.start()
     evs = []
+    if args.profile_range:
+        torch.cuda.profiler.start()
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -355,6 +360,8 @@ def run_ours(args, dist: Dist):
         evs.append((e0, e1))
     ctx.sync()
     torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.stop()
     dist.barrier()
     sampler.stop()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
@@ -362,6 +369,8 @@ def run_ours(args, dist: Dist):
     ctx.profile(False)
     launches = prof["kernel_launches"] - launches0
     value, ms_per_step = aggregate(step_ms, dist)
+    if args.profile_range:  # a profiling run: the captured frames are all it is for
+        return {"profile_range": True, "workload": args.workload, "ms_per_step": round(ms_per_step, 4)}, scene
 
     # ---- timed end to end: uploads from pinned host memory and read-back in the region
     keep = []
@@ -477,12 +486,15 @@ def run_ours(args, dist: Dist):
     return out, scene
 
 
-def timed_steps(stream, flush, steps: int, body):
+def timed_steps(stream, flush, steps: int, body, profile_range: bool = False):
     """K steps of `body`, each bracketed by CUDA events on the library stream after an L2
-    flush (outside the events); returns per-step milliseconds."""
+    flush (outside the events); returns per-step milliseconds. With profile_range the steps
+    run between cudaProfilerStart and cudaProfilerStop."""
     import torch
 
     evs = []
+    if profile_range:
+        torch.cuda.profiler.start()
     for _ in range(steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -492,6 +504,8 @@ def timed_steps(stream, flush, steps: int, body):
         e1.record(stream)
         evs.append((e0, e1))
     torch.cuda.synchronize()
+    if profile_range:
+        torch.cuda.profiler.stop()
     return [a.elapsed_time(b) for a, b in evs]
 
 
@@ -662,7 +676,24 @@ def run_batch(args, dist: Dist):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
     n = len(draws)
 
-    # ---- autotune the per-class raster parameter on this batch, then plan it
+    # ---- the step with the default tuning table and launch form, for comparison
+    form_names = {api.BATCH_PERSISTENT: "persistent", api.BATCH_PHASED: "phased", api.BATCH_BINNED: "binned"}
+    untuned = None
+    if not args.no_autotune and not args.profile_range:
+        b0 = api.Batch(ctx, draws)
+        g0 = api.Graph(ctx).begin()
+        b0.launch()
+        g0.end()
+        for _ in range(3):
+            g0.launch()
+        ctx.sync()
+        ms0 = timed_steps(stream, flush, max(3, args.steps // 2), g0.launch)
+        untuned = {"ms_per_step": round(sum(ms0) / len(ms0), 4), "form": form_names[b0.info()["form"]],
+                   "tuning_small_max_pixels": ctx.tuning(), "tuning_bins": ctx.bin_tuning()}
+        g0.close()
+        b0.close()
+
+    # ---- autotune the per-class raster parameters and the launch form on this batch, then plan it
     tuning = ctx.tuning() if args.no_autotune else api.autotune(ctx, draws, repeats=2)
     if args.form != "auto":
         ctx.batch_form = {"persistent": api.BATCH_PERSISTENT, "phased": api.BATCH_PHASED,
@@ -714,9 +745,12 @@ def run_batch(args, dist: Dist):
     dist.barrier()
     torch.cuda.synchronize()
     sampler.start()
-    step_ms = timed_steps(stream, flush, args.steps, graph.launch)
+    step_ms = timed_steps(stream, flush, args.steps, graph.launch, args.profile_range)
     dist.barrier()
     sampler.stop()
+    if args.profile_range:  # a profiling run: the captured steps are all it is for
+        return {"profile_range": True, "form": info["form"], "ms_per_step": round(sum(step_ms) / len(step_ms), 4),
+                "config": batch_config(args, dist, n)}, scenes
     plain_ms = timed_steps(stream, flush, args.steps, plain_graph.launch)
     # the plain path as a host loop of per-draw calls (no graph), for reference
     eager_ms = timed_steps(stream, flush, max(3, args.steps // 4), lambda: [
@@ -877,6 +911,8 @@ def run_batch(args, dist: Dist):
         + ", replayed from a CUDA graph",
         "tuning_small_max_pixels": tuning,
         "tuning_bins": ctx.bin_tuning(),
+        "untuned": untuned,
+        "tuned_vs_untuned": round(untuned["ms_per_step"] / ms, 3) if untuned else None,
         "gfrag_per_s": round(frags * value / n / 1e9, 3),
         "mtri_per_s": round(faces * value / n / 1e6, 2),
         "fragments_per_step": int(frags), "shaded_per_step": int(st["shaded"]), "tested_per_step": int(st["tested"]),
