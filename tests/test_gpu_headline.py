@@ -4,6 +4,8 @@
   resolution with the eight 1024^2 textures, planned after the autotuner, drawn by the
   batched form. Every draw is compared with the oracle (depth bit-exact, colour within
   1 LSB) and the per-draw differing-pixel counts are printed.
+* The binned and persistent launch forms on the same 512-draw batch, against the phased
+  form bit for bit.
 * The served mix at full size: a 200,000-triangle soup at 3840x2160 and a 2,093,058-
   triangle heightfield at 1920x1080 among small requests, each the same alone and in the
   mix, and the two large requests against the oracle.
@@ -45,6 +47,40 @@ def test_full_mixed_batch_against_oracle(ctx, port):
           f"max {max(differing)}, draws with any {sum(1 for x in differing if x)}")
     batch.close()
     for d in draws:
+        d.framebuffer.close()
+
+
+@pytest.mark.parametrize("form", [api.BATCH_BINNED, api.BATCH_PERSISTENT])
+def test_full_mixed_batch_forms_agree(ctx, form):
+    """The other launch forms on the same 512-draw batch give the phased form's frames bit
+    for bit (the phased form being the one checked against the oracle above when the
+    autotuner picks it; either way every form is pinned at the headline configuration)."""
+    scenes = W.batch_scenes()
+    textures, meshes = {}, {}
+    ref = api.batch_draws(ctx, scenes, textures, meshes)
+    alt = api.batch_draws(ctx, scenes, textures, meshes)
+    saved = ctx.batch_form
+    try:
+        ctx.batch_form = api.BATCH_PHASED
+        b_ref = api.Batch(ctx, ref)
+        ctx.batch_form = form
+        b_alt = api.Batch(ctx, alt)
+    finally:
+        ctx.batch_form = saved
+    for d in alt:
+        d.framebuffer.clearColor(7, 7, 7, 7)
+        d.framebuffer.clearDepth(-1.0)
+    b_ref.launch()
+    b_alt.launch()
+    ctx.sync()
+    for k, (dr, da) in enumerate(zip(ref, alt)):
+        cr, zr = dr.framebuffer.read()
+        ca, za = da.framebuffer.read()
+        assert np.array_equal(cr, ca), f"draw {k}: colour differs in {int((cr != ca).any(axis=2).sum())} pixels"
+        assert np.array_equal(zr.view(np.uint32), za.view(np.uint32)), f"draw {k}: depth differs"
+    b_ref.close()
+    b_alt.close()
+    for d in ref + alt:
         d.framebuffer.close()
 
 
