@@ -641,7 +641,12 @@ __device__ void bin_tile(const DrawParams& p, const BinSet& bs, uint32_t lb, con
         const int ox = tile_x(tid), oy = tile_y(tid);
         if (ox < t.width && oy < t.height) t.tile_flag[(uint32_t)(oy >> 4) * (uint32_t)t.tiles_x + (uint32_t)(ox >> 4)] = 0u;
     }
-    if (!sm.ok) return;  // tile contents unknown: leave the framebuffer as it is
+    if (!sm.ok) {  // tile contents unknown: leave the framebuffer as it is
+        // the CTA's shared memory outlives loads still in flight only while a thread stays:
+        // one more bounded wait for them before the CTA exits
+        if (tid == 0) mbar_wait_bounded(&sm.bar, 0);
+        return;
+    }
     const uint32_t tile_has = sm.tile_has;
 
     // ---- write the tiles out: a plane of a tile is written when it was cleared or the tile
