@@ -2,7 +2,8 @@
 concurrent requests (exactly: the same device functions compute every value), equal to
 the per-draw path and within the parity bar of the oracle; assets are evicted and
 re-uploaded under a small device-memory budget without changing results; per-request
-mode gives the same frames; oversized requests and bad arguments are rejected."""
+mode gives the same frames, and so do slots rendering side by side on their own streams;
+oversized requests and bad arguments are rejected."""
 import numpy as np
 import pytest
 
@@ -105,6 +106,32 @@ def test_per_request_mode_matches(ctx):
         assert res["status"] == AXR_OK
         exp = per_draw(ctx, scenes[k])
         assert np.array_equal(bgra, exp[0]) and np.array_equal(depth.view(np.uint32), exp[1].view(np.uint32))
+    srv.close()
+
+
+@pytest.mark.parametrize("per_request", [False, True])
+@pytest.mark.parametrize("budget", [1 << 30, 3 << 20])
+def test_overlapping_slots_match(ctx, per_request, budget):
+    """overlap_kernels: each in-flight slot renders on its own stream and scratch. Frames
+    equal the per-draw path with a roomy budget and with one that forces framebuffers and
+    assets to be freed and reallocated between the slots' streams."""
+    scenes = scenes_mix()
+    srv = api.Server(0, budget_bytes=budget, max_batch=4, max_inflight=2, per_request=per_request,
+                     overlap_kernels=True)
+    ids = [srv.add_mesh(sc.mesh) for sc in scenes]
+    expect = [per_draw(ctx, sc) for sc in scenes]
+    srv.hold(True)
+    pending = [(k % len(scenes),) + request(srv, ids, scenes[k % len(scenes)], k % len(scenes))
+               for k in range(3 * len(scenes))]
+    srv.hold(False)
+    for k, t, bgra, depth in pending:
+        res = srv.wait(t, 60000)
+        assert res["status"] == AXR_OK, res
+        assert np.array_equal(bgra, expect[k][0]) and np.array_equal(depth.view(np.uint32), expect[k][1].view(np.uint32)), \
+            f"scene {k} differs (batch of {res['batch_size']})"
+    st = srv.stats()
+    if budget < (1 << 30):
+        assert st["evictions"] > 0
     srv.close()
 
 
