@@ -469,12 +469,22 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
     __shared__ uint8_t s_list[kBatchWarps][256];
     __shared__ uint32_t s_n[kBatchWarps], s_buf[kBatchWarps], s_tile[kBatchWarps];
     __shared__ uint32_t s_dirty;
+    __shared__ __align__(128) uint32_t s_clear[2][256];  // a cleared tile: colour, depth (TMA source)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool stats = bp.collect_stats != 0;
     stage_unit(bp, bp.vert_units + bp.face_units + blockIdx.x, &s_p, &s_u);
     __syncthreads();
     const DrawParams& p = s_p;
     const UnitInfo& ui = s_u;
+    // a fully cleared draw with tensor maps: its key-less tiles go out as TMA stores of one
+    // cleared tile in shared memory (no clear kernel; every pixel of the frame written once)
+    const bool tma_clear = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth) &&
+                           (ui.flags & kBatchTma) && !(ui.flags & kBatchClearedApart);
+    if (tma_clear) {
+        s_clear[0][threadIdx.x] = ui.clear_bgra;
+        s_clear[1][threadIdx.x] = __float_as_uint(ui.clear_depth);
+        tma_fence_smem();  // visible to the TMA unit after the barrier below
+    }
     const uint32_t ntiles = (uint32_t)p.target.tiles_x * (uint32_t)p.target.tiles_y;
     const uint32_t unit = kUnitWarps * bp.tiles_per_warp;  // <= 32
     const uint32_t first = ui.local * unit;
@@ -489,14 +499,29 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
     const unsigned dirty = s_dirty;
     const bool clears = (ui.flags & (kBatchClearColor | kBatchClearDepth)) != 0u;
     const bool full = (ui.flags & (kBatchClearColor | kBatchClearDepth)) == (kBatchClearColor | kBatchClearDepth);
-    // key-less tiles with a full clear: direct stores, spread over the warps (unless the
-    // clear kernel has written them already)
+    // key-less tiles with a full clear, spread over the warps (unless the clear kernel has
+    // written them already): TMA stores of the cleared tile, issued by the warp's lane 0 and
+    // read back from shared memory before the CTA exits (one issuing thread per tile
+    // measured 1% slower); direct stores without tensor maps
     if (full && !(ui.flags & kBatchClearedApart)) {
         unsigned clean = all & ~dirty;
+        const BatchDraw* bd = &bp.draws[ui.draw];
         for (int k = 0; clean; ++k) {
             const int t = __ffs(clean) - 1;
             clean &= clean - 1u;
-            if ((k & (kBatchWarps - 1)) == warp) clear_tile(p.target, first + (uint32_t)t, ui.clear_bgra, ui.clear_depth);
+            if ((k & (kBatchWarps - 1)) != warp) continue;
+            const uint32_t tile = first + (uint32_t)t;
+            if (tma_clear) {
+                if (lane == 0) {
+                    const int x = (int)(tile % (uint32_t)p.target.tiles_x) * kTile;
+                    const int y = (int)(tile / (uint32_t)p.target.tiles_x) * kTile;
+                    tma_store_tile(&bd->color_map, s_clear[0], x, y);
+                    tma_store_tile(&bd->depth_map, s_clear[1], x, y);
+                    tma_commit();
+                }
+            } else {
+                clear_tile(p.target, tile, ui.clear_bgra, ui.clear_depth);
+            }
         }
     }
     // staged tiles: the dirty ones, plus the key-less ones when only one plane is cleared
@@ -541,8 +566,9 @@ __global__ void __launch_bounds__(kBatchBlock, AXR_TILE_MIN_BLOCKS) batch_tile_k
         if (mine >= 0 && tile_finish<S>(p, ui, &bp.draws[ui.draw], c, stage, s_list[warp], n >> 16)) sbuf ^= 1u;
         __syncthreads();  // s_list, s_n, s_buf and s_tile are rewritten by the next round
     }
-    // the staging buffers must have been read before the CTA exits
-    if (lane == 0) tma_wait_read_0();
+    // the staging buffers and the cleared tile must have been read before the CTA exits
+    // (a thread that committed no store group passes at once)
+    tma_wait_read_0();
 }
 
 // Clear of both planes of the phased form's fully cleared draws, in spans of kClearUnit

@@ -183,7 +183,8 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             total_units += (uint64_t)bplan[(size_t)i].bins_x * bplan[(size_t)i].bins_y;
         else if (drawn || (d.clear_flags & (AXR_DRAW_CLEAR_COLOR | AXR_DRAW_CLEAR_DEPTH)))
             total_units += ceil_div((uint64_t)d.framebuffer->tiles_x * d.framebuffer->tiles_y, tile_unit);
-        if (form == kFormPhased && (d.clear_flags & AXR_DRAW_CLEAR_COLOR) && (d.clear_flags & AXR_DRAW_CLEAR_DEPTH))
+        if (form == kFormPhased && (d.clear_flags & AXR_DRAW_CLEAR_COLOR) && (d.clear_flags & AXR_DRAW_CLEAR_DEPTH) &&
+            !d.framebuffer->tma)
             total_units += ceil_div((uint64_t)d.framebuffer->width * d.framebuffer->height, kClearUnit);
     }
     const size_t table_bytes = align256(sizeof(BatchDraw) * (size_t)std::max(count, 1));
@@ -305,9 +306,10 @@ axr_status plan_batch(axr_context* ctx, const axr_draw_desc* draws, int32_t coun
             for (uint32_t j = 0; j < nv; ++j) uv.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nf; ++j) uf.push_back(UnitRef{(uint32_t)k, j});
             for (uint32_t j = 0; j < nt; ++j) ut.push_back(UnitRef{(uint32_t)k, j});
-            // the phased form clears both planes of a fully cleared draw in its own kernel
-            // before the other phases
-            if (form == kFormPhased && (bd.flags & kBatchClearColor) && (bd.flags & kBatchClearDepth)) {
+            // the phased form clears both planes of a fully cleared draw in its tile pass:
+            // the key-less tiles with TMA stores of a cleared tile. A framebuffer without
+            // tensor maps (width not a multiple of 4) is cleared by its own kernel first.
+            if (form == kFormPhased && (bd.flags & kBatchClearColor) && (bd.flags & kBatchClearDepth) && !fb->tma) {
                 bd.flags |= kBatchClearedApart;
                 const uint32_t nc = ceil_div((uint64_t)fb->width * fb->height, kClearUnit);
                 for (uint32_t j = 0; j < nc; ++j) uc.push_back(UnitRef{(uint32_t)k, j});

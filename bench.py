@@ -555,26 +555,29 @@ def binned_phase_bytes(scenes, shaded: float) -> dict:
     return {"clear": 0.0, "vertex": 32.0 * v, "face": 12.0 * f, "large": 0.0, "tile": 8.0 * px + tex}
 
 
-def batch_phase_bytes(scenes, frags: float, tiles: int, dirty: int, clear_apart: bool) -> dict:
+def batch_phase_bytes(scenes, frags: float, tiles: int, dirty: int, phased: bool) -> dict:
     """Algorithmic bytes of each phase of one batched step (Blinn-Phong: 48-byte vertex
     cache entries): vertices read (32) + cache written (48) per vertex; indices (12 per
     face) + cache gathers (16 per vertex) + one key per covered fragment (8) for the face
     and large phases together; the tile pass reads the flags (4 per tile), reads and resets
     the key of every covered pixel (16), reads the vertex cache (48 per vertex) and
-    min(texture, 4 per covered fragment), and writes colour + depth (8 per pixel): of the
-    dirty tiles when the clear kernel has written every pixel before (its own 8 per pixel),
-    of every pixel otherwise."""
+    min(texture, 4 per covered fragment), and writes colour + depth (8 per pixel) of every
+    pixel, except in the phased form for framebuffers without tensor maps (width not a
+    multiple of 4): a clear kernel writes those (its own 8 per pixel) and the tile pass
+    only their dirty tiles."""
     total_faces = sum(int(sc.mesh.indices.shape[0]) for sc in scenes)
-    v = f = px = tex = 0.0
+    v = f = px = tex = apart = 0.0
     for sc in scenes:
         V, F = sc.mesh.positions.shape[0], sc.mesh.indices.shape[0]
         t = sum(int(m.diffuse.nbytes) for m in sc.mesh.materials if m.diffuse is not None)
         v += V
         f += F
         px += sc.width * sc.height
+        if phased and sc.width % 4 != 0:
+            apart += sc.width * sc.height
         tex += min(t, 4.0 * frags * F / max(1, total_faces))
-    written = 8.0 * 256 * dirty if clear_apart else 8.0 * px
-    return {"clear": 8.0 * px if clear_apart else 0.0, "vertex": 80.0 * v,
+    written = 8.0 * (px - apart) + (8.0 * 256 * dirty * apart / px if px else 0.0)
+    return {"clear": 8.0 * apart, "vertex": 80.0 * v,
             "face": 12.0 * f + 16.0 * v + 8.0 * frags, "large": 8.0 * frags,
             "tile": written + 4.0 * tiles + 16.0 * frags + 48.0 * v + tex}
 
@@ -902,10 +905,12 @@ def run_batch(args, dist: Dist):
                       "shading the winners and writing colour and depth once with TMA stores, clears fused)"
                       + (", as two launch sets of alternating draws on two streams" if info["launches"] > 1 else "")
                       if info["form"] == 2 else
-                      "batched, phased: a clear kernel and four phase launches over the work units of "
+                      "batched, phased: four phase launches (the tile pass also clearing the key-less tiles "
+                      "with TMA stores) over the work units of "
                       "all draws, as two launch sets of alternating draws on two streams"
                       if info["form"] == 1 and info["launches"] > 1 else
-                      "batched, phased: a clear kernel and four phase launches per step over the work "
+                      "batched, phased: four phase launches per step (the tile pass also clearing the "
+                      "key-less tiles with TMA stores) over the work "
                       "units of all draws" if info["form"] == 1 else
                       "batched, persistent: one cooperative launch per step (clears fused into the tile pass)")
         + ", replayed from a CUDA graph",

@@ -37,7 +37,7 @@ def test_our_arm_line_on_a_reduced_batch():
             "e2e_rgb"} <= set(d)
     r = d["roofline"]
     assert r["bound"] == "hbm" and 0 < r["frac"] < 2 and r["peak"] > 0 and r["achieved"] > 0
-    # phased: clear, vertex, face, large, tile per step; binned: vertex, face, bin;
-    # persistent: one cooperative launch
-    assert d["gpu_launches"] in (3 * 5, 3 * 3, 3 * 1)
+    # phased: vertex, face, large, tile per step (a clear kernel too for framebuffers
+    # without tensor maps); binned: vertex, face, bin; persistent: one cooperative launch
+    assert d["gpu_launches"] in (3 * 5, 3 * 4, 3 * 3, 3 * 1)
     assert d["e2e"]["d2h_bytes_per_step"] > 0 and d["e2e"]["value"] > 0
