@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import os
 import statistics
@@ -1052,6 +1053,10 @@ def serve_sweep(device: int, rates, seconds: float, budget_gb: float, readback: 
             which = rng.integers(0, len(reqs), n)
             az = rng.random(n) * 360.0
             tickets = [None] * n
+            # the submitting loop must not pause: a garbage collection inside it would delay
+            # submissions and show up as request latency (arrivals are scheduled, open loop)
+            gc.collect()
+            gc.disable()
             t0 = srv.now_ns() + 2_000_000
             k = 0
             slot = hf_slot = 0
@@ -1072,6 +1077,7 @@ def serve_sweep(device: int, rates, seconds: float, budget_gb: float, readback: 
                     wait = (t0 + int(offs[k]) - srv.now_ns()) / 1e9
                     if wait > 2e-4:
                         time.sleep(wait - 1e-4)
+            gc.enable()
             lat, sizes, last, fails = [], [], 0, 0
             for t in tickets:
                 r = srv.wait(t)
