@@ -130,6 +130,34 @@ def test_batch_odd_widths_without_tma(ctx):
         assert_same(got[k], exp[k], f"odd width draw {k}")
 
 
+def test_phased_clears_with_and_without_tensor_maps(ctx):
+    """The phased form's fused clears: framebuffers with tensor maps get their key-less
+    tiles from TMA stores of a cleared tile in the tile pass, the others from the clear
+    kernel; both in one batch, over framebuffers scribbled beforehand, with partial edge
+    tiles and a draw whose mesh covers little of its frame, equal the per-draw path."""
+    sizes = ((256, 131, 32), (250, 131, 24), (100, 37, 16), (97, 203, 40), (512, 64, 8), (36, 300, 64))
+    scenes = [W.sphere_scene(width=w, height=h, lon=lon, lat=lon // 2, tex_size=32) for (w, h, lon) in sizes]
+    scenes[4].camera = W.orbit_camera(12.0, 10.0, 30.0, 512, 64)  # far away: mostly key-less tiles
+    draws = api.batch_draws(ctx, scenes)
+    for d in draws:
+        d.clear_color = (10, 20, 30, 40)
+        d.clear_depth = 0.75
+        d.framebuffer.clearColor(200, 1, 2, 3)
+        d.framebuffer.clearDepth(-5.0)
+    saved = ctx.batch_form
+    try:
+        ctx.batch_form = api.BATCH_PHASED
+        b = api.Batch(ctx, draws)
+    finally:
+        ctx.batch_form = saved
+    b.launch()
+    got = [d.framebuffer.read() for d in draws]
+    exp = plain_frames(ctx, scenes, draws)
+    for k in range(len(scenes)):
+        assert_same(got[k], exp[k], f"draw {k} ({sizes[k][0]}x{sizes[k][1]})")
+    b.close()
+
+
 def test_batch_all_shader_kinds(ctx, port):
     """Flat, Phong, PBR, Blinn-Phong and Gouraud draws in one batch: one launch per kind."""
     scenes = []
