@@ -296,9 +296,10 @@ __device__ __forceinline__ f4 fragment_shader(const DevUniforms& u, const DevMat
 }
 
 // (uint8_t)(std::clamp(c, 0, 1) * 255): truncating conversion, NaN -> 0.
+// __saturatef clamps to [0, 1] and maps NaN to 0, which is the clamp followed by the NaN
+// rule; the product is then in [0, 255] and truncates to the byte.
 __device__ __forceinline__ uint32_t quantize(float c) {
-    float v = fmul(sclamp(c, 0.0f, 1.0f), 255.0f);
-    return v == v ? (uint32_t)__float2uint_rz(v) & 0xFFu : 0u;
+    return (uint32_t)__float2uint_rz(fmul(__saturatef(c), 255.0f));
 }
 
 // RGBA floats -> framebuffer word with bytes B, G, R, A (reference
