@@ -895,6 +895,10 @@ def run_batch(args, dist: Dist):
                  "large": "batch_large_kernel", "tile": "batch_tile_kernel"} if info["form"] == 1 else \
         {k: "batch_kernel" for k in phase_ms}
     dom_achieved = pb[dom] / (phase_ms[dom] * 1e-3) / 1e9 if phase_ms[dom] > 0 else 0.0
+    # the same pass on the frame's own bytes only (colour + depth of every pixel it writes
+    # and the texels), without the design's intermediate data (keys, flags, vertex cache)
+    frame_only = binned_phase_bytes(scenes, float(st["shaded"]))["tile"] if dom == "tile" else pb[dom]
+    frame_only_achieved = frame_only / (phase_ms[dom] * 1e-3) / 1e9 if phase_ms[dom] > 0 else 0.0
     out = {
         "metric": "frames/s", "value": round(value, 2), "unit": "frames/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -959,6 +963,7 @@ def run_batch(args, dist: Dist):
                      "peak": hbm_peak, "peak_source": peak_kind, "unit": "GB/s",
                      "frac": round(dom_achieved / hbm_peak, 4), "traffic": profiled_traffic(kernel_of[dom], "batch"),
                      "algorithmic_bytes": pb[dom], "kernel_us_per_step": round(phase_ms[dom] * 1e3, 2),
+                     "frame_bytes_only": frame_only, "frac_frame_bytes_only": round(frame_only_achieved / hbm_peak, 4),
                      "launches_per_step": launches_per_step,
                      "per": "step: algorithmic bytes, traffic and kernel time summed over the step's launches "
                             "of the kernel (one per launch set)",
