@@ -53,6 +53,40 @@ void dfree(void* p) {
     if (p) cudaFree(p);
 }
 
+// Whether no vertex of the mesh can lie outside or on any of the six clip planes
+// (x+w, w-x, y+w, w-y, z+w, w-z >= 0 of clip = mvp * (p, 1)) for the column-major mvp: the
+// smallest value of each plane's function over the mesh's bounding sphere, in double, must
+// exceed a margin far above the rounding of the device's float evaluation. Unknown bounds
+// (an update still in flight) or non-finite values answer false.
+bool mesh_clip_free(const axr_mesh* m, const float mvp[16]) {
+    if (!m || m->num_vertices == 0) return false;
+    if (m->bounds_pending) {
+        if (cudaEventQuery(m->bounds_ready) != cudaSuccess) {
+            cudaGetLastError();  // cudaErrorNotReady is no error here
+            return false;
+        }
+        mesh_sync_bounds(m);
+        if (m->bounds_pending) return false;
+    }
+    const double c[3] = {m->bound_center[0], m->bound_center[1], m->bound_center[2]};
+    const double r = m->bound_radius;
+    const double extent = std::max({std::fabs(c[0]), std::fabs(c[1]), std::fabs(c[2])}) + r + 1.0;
+    for (int k = 0; k < 6; ++k) {
+        const int j = k / 2;                       // the x, y or z row of the matrix
+        const double s = (k % 2 == 0) ? 1.0 : -1.0;  // w + row or w - row
+        double g[3], norm2 = 0.0, terms = 0.0;
+        for (int i = 0; i < 3; ++i) {
+            g[i] = (double)mvp[4 * i + 3] + s * (double)mvp[4 * i + j];
+            norm2 += g[i] * g[i];
+        }
+        const double h = (double)mvp[12 + 3] + s * (double)mvp[12 + j];
+        for (int i = 0; i < 4; ++i) terms += std::fabs((double)mvp[4 * i + 3]) + std::fabs((double)mvp[4 * i + j]);
+        const double lowest = g[0] * c[0] + g[1] * c[1] + g[2] * c[2] + h - r * std::sqrt(norm2);
+        if (!(lowest > 1e-5 * terms * extent)) return false;
+    }
+    return true;
+}
+
 void mesh_sync_bounds(const axr_mesh* m) {
     static std::mutex mu;  // planners on several threads may share a mesh
     if (!m) return;
@@ -966,7 +1000,9 @@ axr_status axr_draw_mesh(axr_context* ctx, const axr_mesh* mesh, const float mod
         ctx->events_used += kStageEvents;
     }
     if (ctx->draw_form != AXR_DRAW_BINNED) {
-        AXR_CUDA(ctx, launch_draw(p, ctx->cfg, ctx->stream, &ctx->aux, ev, &ctx->launches));
+        LaunchConfig cfg = ctx->cfg;
+        cfg.clip_free = mesh_clip_free(mesh, u.mvp);
+        AXR_CUDA(ctx, launch_draw(p, cfg, ctx->stream, &ctx->aux, ev, &ctx->launches));
         return AXR_OK;
     }
     SoloBinned sb{};

@@ -325,21 +325,25 @@ cudaError_t launch_shaded(const DrawParams& p, const LaunchConfig& cfg, cudaStre
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = mark(4)) != cudaSuccess) return e;
     // the clipped-winner pass is independent of the main shading pass: run it beside it
+    // (unless no triangle can have been clipped, when its list is empty)
+    const bool clipped = !cfg.clip_free;
     cudaStream_t side = aux ? aux->stream : stream;
-    if (aux) {
+    if (clipped && aux) {
         if ((e = cudaEventRecord(aux->fork, stream)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(aux->stream, aux->fork, 0)) != cudaSuccess) return e;
     }
-    resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms / 2u + 1u, kBlock, 0, side>>>(p);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (clipped) {
+        resolve_clipped_kernel<S><<<(unsigned)cfg.num_sms / 2u + 1u, kBlock, 0, side>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     shade_kernel<S><<<(unsigned)(cfg.num_sms * cfg.resolve_ctas_per_sm), kBlock, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = mark(5)) != cudaSuccess) return e;
-    if (aux) {
+    if (clipped && aux) {
         if ((e = cudaEventRecord(aux->join, aux->stream)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(stream, aux->join, 0)) != cudaSuccess) return e;
     }
-    *launches += 4;
+    *launches += clipped ? 4 : 3;
     return mark(6);
 }
 

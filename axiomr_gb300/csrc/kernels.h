@@ -18,6 +18,9 @@ struct LaunchConfig {
     int num_sms;
     int large_ctas_per_sm;
     int resolve_ctas_per_sm;
+    // no vertex of the draw can lie outside or on a clip plane (checked on the host from the
+    // mesh's bounding sphere): no triangle is clipped, so the clipped-winner pass is not run
+    bool clip_free = false;
 };
 
 // One draw: geometry (transform, clip, cull, setup, small-triangle raster) -> large

@@ -150,3 +150,20 @@ def test_empty_and_offscreen_meshes(ctx, port):
     behind = dataclasses.replace(sc, camera=W.Camera((0.0, 0.0, 3.0), (0.0, 0.0, 6.0), 60.0, 1.0, (0, 0, 64, 64)))
     got = api.render_scene(ctx, behind, framebuffer=fb)
     assert np.isinf(got[1]).all()
+
+
+def test_clipped_winner_pass_skipped_only_when_nothing_can_clip(ctx, port):
+    """A mesh whose bounding sphere lies inside all six clip planes cannot have clipped
+    triangles: its draw runs without the clipped-winner pass (one launch fewer). The same
+    mesh crossing the near plane runs it, and both frames match the oracle."""
+    sc = W.sphere_scene(width=160, height=120, lon=24, lat=12)
+    near = W.sphere_scene(width=160, height=120, lon=24, lat=12)
+    near.camera = W.orbit_camera(1.05, 0.0, 0.0, 160, 120)  # the unit sphere reaches the near plane
+    launches = []
+    for s in (sc, near):
+        ctx.sync()
+        k0 = ctx.profile()["kernel_launches"]
+        got = api.render_scene(ctx, s)
+        launches.append(ctx.profile()["kernel_launches"] - k0)
+        assert_parity(got, port.draw(s, port.camera(s.camera)[2]), "sphere")
+    assert launches[0] == launches[1] - 1, launches
